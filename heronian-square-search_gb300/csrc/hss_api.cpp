@@ -1,0 +1,817 @@
+// hss_api.cpp - C ABI over the sm_103a search kernels (include/hss.h).
+//
+// Replaces the reference's in-process boundary: Search::prepare builds the
+// factor cache (gpu_search_v42.cu:354-391), Search::run uploads it and loops
+// launch / synchronise / harvest over batches of at most 512 roots
+// (gpu_search_v42.cu:393-495).  Here the cache is built once per handle on all
+// host threads and stays resident; each search call is one launch sequence on
+// a private stream (batched: items built on the host, one persistent launch,
+// one shared-prime launch; plain: one launch per <= 512 roots), timed with
+// CUDA events, and its counters and hits are copied back once.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+#include <time.h>
+
+#include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "hss_api_status.h"
+#include "hss_kernels.h"
+#include "hss_prep.h"
+
+using namespace hss;
+
+namespace {
+
+constexpr uint32_t kDefaultHitCap = 4096;      // gpu_search_v42.cu:177-178
+constexpr uint32_t kPlainBatch = 512;          // gpu_search_v42.cu:457
+constexpr uint32_t kDefaultItemTarget = 1u << 20;
+constexpr uint32_t kTileCap = 1024;            // largest m-range of one item
+constexpr uint32_t kTileMin = 32;
+constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
+constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
+
+struct Request;
+
+}  // namespace
+
+struct hss_ctx {
+    int device = 0;
+    uint64_t limit = 0;
+    hss_opts opts{};
+    int sm_count = 0;
+    std::string err;
+
+    // host mirrors used to build work items
+    std::vector<uint32_t> seg_off;
+    std::vector<uint32_t> spf;
+    uint64_t records = 0, ref_flattened = 0, ref_cached = 0;
+    double prep_seconds = 0;
+
+    DeviceCache dev{};
+    std::vector<void*> allocations;
+
+    // launch buffers
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    RowCounts* d_rows = nullptr;
+    size_t rows_cap = 0;
+    DevHit* d_hits = nullptr;
+    uint32_t hit_cap = 0;
+    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags
+    uint4* d_merged = nullptr;
+    uint32_t merged_cap = 0;
+    uint8_t* d_tables = nullptr;
+    WorkItem* d_items = nullptr;
+    size_t items_cap = 0;
+    WorkItem* h_items = nullptr;  // pinned
+    size_t h_items_cap = 0;
+    RowCounts* h_rows = nullptr;  // pinned
+    size_t h_rows_cap = 0;
+
+    std::mutex gpu_mu;  // serialises device work on the handle
+
+    // serving
+    std::mutex serve_mu;
+    std::condition_variable serve_cv;
+    std::thread serve_thread;
+    bool serving = false, serve_stop = false;
+    uint32_t max_active = 0, wave_items = 0;
+    uint64_t next_id = 1;
+    std::map<uint64_t, Request*> requests;
+    std::deque<uint64_t> pending;
+};
+
+namespace {
+
+std::mutex g_err_mu;
+
+int fail(hss_t* h, int status, const std::string& msg) {
+    if (h) h->err = msg;
+    return status;
+}
+
+#define HSS_CUDA(h, call)                                                                      \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(h, HSS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+uint64_t now_ns() {
+    timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (uint64_t)ts.tv_sec * 1000000000ull + (uint64_t)ts.tv_nsec;
+}
+
+template <class T>
+int device_alloc(hss_t* h, T** out, size_t count) {
+    void* p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) return fail(h, HSS_ERR_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    h->allocations.push_back(p);
+    *out = static_cast<T*>(p);
+    return HSS_OK;
+}
+
+void device_free(hss_t* h, void* p) {
+    if (!p) return;
+    auto it = std::find(h->allocations.begin(), h->allocations.end(), p);
+    if (it != h->allocations.end()) h->allocations.erase(it);
+    cudaFree(p);
+}
+
+template <class T>
+int upload(hss_t* h, T** out, const T* src, size_t count) {
+    int s = device_alloc(h, out, count);
+    if (s) return s;
+    HSS_CUDA(h, cudaMemcpy(*out, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return HSS_OK;
+}
+
+uint32_t free_count(const hss_t* h, uint64_t x) { return h->seg_off[x + 1] - h->seg_off[x] - 1; }
+
+// Upper bound on the pairs of row l that share a split prime with m in
+// [l, N]: inclusion-exclusion over the distinct split primes of l.
+uint64_t merged_bound(const hss_t* h, uint64_t l) {
+    NumberFactors f = factor_number(h->spf.data(), l);
+    if (f.count == 0) return 0;
+    uint64_t n = h->limit, total = 0;
+    for (uint32_t mask = 1; mask < (1u << f.count); ++mask) {
+        uint64_t prod = 1;
+        int bits = 0;
+        bool over = false;
+        for (uint32_t i = 0; i < f.count; ++i)
+            if (mask & (1u << i)) {
+                prod *= f.primes[i];
+                ++bits;
+                if (prod > n) over = true;
+            }
+        if (over) continue;
+        uint64_t cnt = n / prod - (l - 1) / prod;
+        if (bits & 1) total += cnt;
+        else total -= cnt;
+    }
+    return total;
+}
+
+int ensure_rows(hss_t* h, size_t rows) {
+    if (rows <= h->rows_cap) return HSS_OK;
+    device_free(h, h->d_rows);
+    h->d_rows = nullptr;
+    size_t cap = std::max(rows, (size_t)1024);
+    int s = device_alloc(h, &h->d_rows, cap);
+    if (s) return s;
+    h->rows_cap = cap;
+    if (h->h_rows) cudaFreeHost(h->h_rows);
+    h->h_rows = nullptr;
+    HSS_CUDA(h, cudaMallocHost(&h->h_rows, cap * sizeof(RowCounts)));
+    h->h_rows_cap = cap;
+    return HSS_OK;
+}
+
+int ensure_items(hss_t* h, size_t n) {
+    if (n > h->items_cap) {
+        device_free(h, h->d_items);
+        h->d_items = nullptr;
+        size_t cap = std::max(n + n / 4, (size_t)1 << 16);
+        int s = device_alloc(h, &h->d_items, cap);
+        if (s) return s;
+        h->items_cap = cap;
+    }
+    if (n > h->h_items_cap) {
+        if (h->h_items) cudaFreeHost(h->h_items);
+        h->h_items = nullptr;
+        size_t cap = std::max(n + n / 4, (size_t)1 << 16);
+        HSS_CUDA(h, cudaMallocHost(&h->h_items, cap * sizeof(WorkItem)));
+        h->h_items_cap = cap;
+    }
+    return HSS_OK;
+}
+
+LaunchBuffers buffers(const hss_t* h, size_t row_offset) {
+    LaunchBuffers b;
+    b.rows = h->d_rows + row_offset;
+    b.hits = h->d_hits;
+    b.hit_count = h->d_ctrl + 0;
+    b.hit_cap = h->hit_cap;
+    b.merged_queue = h->d_merged;
+    b.merged_count = h->d_ctrl + 1;
+    b.merged_cap = h->merged_cap;
+    b.next_item = h->d_ctrl + 2;
+    b.error_flags = h->d_ctrl + 3;
+    b.tables = h->d_tables;
+    return b;
+}
+
+// A row of a launch: root l and its index in the call's row counters.
+struct RowRef {
+    uint64_t l;
+    uint32_t index;
+};
+
+// Work items of the given rows: each row's m-range [l, N] cut into ranges of
+// about item_target alpha*beta evaluations (at most kTileCap roots), then
+// ordered by m so that concurrently running items read the same m-side
+// records from L2.  Returns the largest row segment and m-range.
+size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap, uint32_t* tile_cap) {
+    const uint64_t n = h->limit;
+    const uint32_t target = h->opts.item_target ? h->opts.item_target : kDefaultItemTarget;
+    std::vector<uint32_t> tile(nrows);
+    size_t total = 0;
+    uint32_t acap = 1, tcap = kTileMin;
+    for (size_t r = 0; r < nrows; ++r) {
+        uint64_t l = rows[r].l;
+        uint32_t na = free_count(h, l) + 1;
+        acap = std::max(acap, na);
+        double per_m = (double)(h->seg_off[n + 1] - h->seg_off[l]) / (double)(n - l + 1);
+        double t = (double)target / ((double)na * std::max(per_m, 1.0));
+        uint32_t tm = t >= kTileCap ? kTileCap : (uint32_t)t;
+        tm = std::max(kTileMin, tm & ~(kTileMin - 1));
+        tile[r] = tm;
+        tcap = std::max(tcap, tm);
+        total += (n - l + 1 + tm - 1) / tm;
+    }
+    if (ensure_items(h, total)) return (size_t)-1;
+    // counting sort by m-bucket of the item start
+    const size_t nb = (n >> kBucketShift) + 2;
+    std::vector<uint32_t> count(nb + 1, 0);
+    for (size_t r = 0; r < nrows; ++r)
+        for (uint64_t m = rows[r].l; m <= n; m += tile[r]) ++count[(m >> kBucketShift) + 1];
+    for (size_t b = 1; b <= nb; ++b) count[b] += count[b - 1];
+    for (size_t r = 0; r < nrows; ++r) {
+        uint64_t l = rows[r].l;
+        for (uint64_t m = l; m <= n; m += tile[r]) {
+            uint64_t m1 = std::min<uint64_t>(m + tile[r], n + 1);
+            h->h_items[count[m >> kBucketShift]++] =
+                WorkItem{(uint32_t)l, (uint32_t)m, (uint32_t)m1, rows[r].index};
+        }
+    }
+    *alpha_cap = acap;
+    *tile_cap = tcap;
+    return total;
+}
+
+[[maybe_unused]] int check_errors(hss_t* h) {
+    unsigned int ctrl[4];
+    HSS_CUDA(h, cudaMemcpy(ctrl, h->d_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost));
+    if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
+    if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
+    return HSS_OK;
+}
+
+// Launches the batched sequence for a set of rows whose shared-prime pairs
+// fit the queue: reset cursor/queue, items H2D, persistent kernel, shared-prime
+// kernel.  Counters accumulate into d_rows[index].
+int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
+    uint32_t acap = 1, tcap = kTileMin;
+    size_t n_items = build_items(h, rows, nrows, &acap, &tcap);
+    if (n_items == (size_t)-1) return HSS_ERR_MEMORY;
+    if (n_items == 0) return HSS_OK;
+    HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                                h->stream));
+    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
+    BatchedConfig cfg;
+    cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
+    cfg.alpha_cap = acap;
+    cfg.tile_cap = tcap;
+    size_t smem = batched_smem_bytes(acap, tcap);
+    int per_sm = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : batched_max_ctas_per_sm(cfg.threads, smem);
+    cfg.ctas = h->sm_count * per_sm;
+    LaunchBuffers b = buffers(h, 0);
+    HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
+    HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 8, h->stream));
+    return HSS_OK;
+}
+
+// Splits rows into groups whose shared-prime bound fits the queue.
+int run_batched(hss_t* h, const std::vector<RowRef>& rows) {
+    size_t start = 0;
+    while (start < rows.size()) {
+        uint64_t bound = 0;
+        size_t end = start;
+        while (end < rows.size()) {
+            uint64_t b = merged_bound(h, rows[end].l);
+            if (end > start && bound + b > h->merged_cap) break;
+            bound += b;
+            ++end;
+        }
+        if (bound > h->merged_cap) return fail(h, HSS_ERR_OVERFLOW, "row exceeds the shared-prime queue");
+        int s = run_batched_rows(h, rows.data() + start, end - start);
+        if (s) return s;
+        start = end;
+    }
+    return HSS_OK;
+}
+
+int run_plain(hss_t* h, uint64_t first, uint64_t last) {
+    for (uint64_t b = first; b <= last; b += kPlainBatch) {
+        uint32_t nrows = (uint32_t)std::min<uint64_t>(kPlainBatch, last - b + 1);
+        uint64_t bound = 0;
+        uint32_t acap = 1;
+        for (uint64_t l = b; l < b + nrows; ++l) {
+            bound += merged_bound(h, l);
+            acap = std::max(acap, free_count(h, l) + 1);
+        }
+        if (bound > h->merged_cap) return fail(h, HSS_ERR_OVERFLOW, "plain batch exceeds the shared-prime queue");
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, sizeof(unsigned int), h->stream));
+        LaunchBuffers buf = buffers(h, b - first);
+        HSS_CUDA(h, launch_plain(h->dev, b, nrows, acap, buf, h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, 0, buf, h->sm_count * 8, h->stream));
+    }
+    return HSS_OK;
+}
+
+int begin_call(hss_t* h, size_t rows) {
+    int s = ensure_rows(h, rows);
+    if (s) return s;
+    HSS_CUDA(h, cudaMemsetAsync(h->d_rows, 0, rows * sizeof(RowCounts), h->stream));
+    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl, 0, 4 * sizeof(unsigned int), h->stream));
+    HSS_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+    return HSS_OK;
+}
+
+// Copies row counters and hits back; hits sorted by (l, m, n) and deduplicated.
+int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint32_t* found) {
+    HSS_CUDA(h, cudaEventRecord(h->ev1, h->stream));
+    HSS_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_rows, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost,
+                                h->stream));
+    unsigned int ctrl[4];
+    HSS_CUDA(h, cudaMemcpyAsync(ctrl, h->d_ctrl, sizeof ctrl, cudaMemcpyDeviceToHost, h->stream));
+    HSS_CUDA(h, cudaStreamSynchronize(h->stream));
+    float f = 0;
+    HSS_CUDA(h, cudaEventElapsedTime(&f, h->ev0, h->ev1));
+    *ms = f;
+    if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
+    if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
+    uint32_t nh = std::min(ctrl[0], h->hit_cap);
+    hits->resize(nh);
+    if (nh) HSS_CUDA(h, cudaMemcpy(hits->data(), h->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
+    std::sort(hits->begin(), hits->end(), [](const DevHit& a, const DevHit& b) {
+        if (a.l != b.l) return a.l < b.l;
+        if (a.m != b.m) return a.m < b.m;
+        return a.n < b.n;
+    });
+    hits->erase(std::unique(hits->begin(), hits->end(),
+                            [](const DevHit& a, const DevHit& b) { return a.l == b.l && a.m == b.m && a.n == b.n; }),
+                hits->end());
+    *found = ctrl[0] > h->hit_cap ? ctrl[0] : (uint32_t)hits->size();
+    return HSS_OK;
+}
+
+void add_row(hss_counts* c, const RowCounts& r) {
+    c->processed += r.processed;
+    c->products += r.products;
+    c->candidates += r.candidates;
+    c->r16 += r.r16;
+    c->exact += r.exact;
+    c->merged += r.merged;
+}
+
+void copy_hits(const std::vector<DevHit>& in, hss_hit* out, uint32_t cap) {
+    for (size_t i = 0; i < in.size() && i < cap; ++i) {
+        out[i].l = in[i].l;
+        out[i].m = in[i].m;
+        out[i].n = in[i].n;
+        out[i].area4_lo = in[i].area4_lo;
+        out[i].area4_hi = in[i].area4_hi;
+        out[i].heron_ok = in[i].heron_ok;
+        out[i].reserved = 0;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ exports
+
+extern "C" {
+
+const char* hss_version(void) { return "hss-gb300 1.0 (sm_103a)"; }
+
+const char* hss_strerror(int status) {
+    switch (status) {
+        case HSS_OK: return "ok";
+        case HSS_ERR_ARGUMENT: return "invalid argument";
+        case HSS_ERR_CUDA: return "CUDA error";
+        case HSS_ERR_MEMORY: return "out of memory";
+        case HSS_ERR_LIMIT: return "limit not supported";
+        case HSS_ERR_STATE: return "checkpoint does not match requested range";
+        case HSS_ERR_OVERFLOW: return "internal capacity exceeded";
+        case HSS_ERR_NOT_FOUND: return "unknown request";
+        case HSS_ERR_BUSY: return "request still running";
+        case HSS_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* hss_last_error(const hss_t* h) { return h ? h->err.c_str() : "null handle"; }
+
+int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
+    if (!out) return HSS_ERR_ARGUMENT;
+    *out = nullptr;
+    if (limit < 1 || limit > HSS_MAX_LIMIT) return HSS_ERR_LIMIT;
+    hss_t* h = new hss_t();
+    if (opts) h->opts = *opts;
+    h->device = device;
+    h->limit = limit;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        delete h;
+        return HSS_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaSetDevice(device) != cudaSuccess || cudaGetDeviceProperties(&prop, device) != cudaSuccess ||
+        prop.major != 10 || prop.minor != 3) {
+        delete h;
+        return HSS_ERR_NO_DEVICE;
+    }
+    h->sm_count = prop.multiProcessorCount;
+    int s = HSS_OK;
+    {
+        HostCache hc;
+        std::string err;
+        unsigned hw = std::thread::hardware_concurrency();
+        int threads = h->opts.prep_threads ? (int)h->opts.prep_threads : (int)(hw ? hw : 1);
+        s = build_host_cache(limit, threads, &hc, &err);
+        if (s) {
+            delete h;
+            return s;
+        }
+        h->records = hc.records;
+        h->ref_flattened = hc.reference_flattened;
+        h->ref_cached = hc.reference_cached;
+        h->prep_seconds = hc.seconds;
+        uint32_t *spf, *seg, *owner, *ppb;
+        HotRec *hot, *pph;
+        ExactRec* ex;
+        __int128* ppx;
+        if ((s = upload(h, &spf, hc.spf.data(), hc.spf.size())) ||
+            (s = upload(h, &seg, hc.seg_off.data(), hc.seg_off.size())) ||
+            (s = upload(h, &hot, hc.hot.get(), hc.records)) || (s = upload(h, &ex, hc.exact.get(), hc.records)) ||
+            (s = upload(h, &owner, hc.owner.get(), hc.records)) ||
+            (s = upload(h, &ppb, hc.pp_base.data(), hc.pp_base.size())) ||
+            (s = upload(h, &pph, hc.pp_hot.data(), hc.pp_hot.size())) ||
+            (s = upload(h, &ppx, hc.pp_exact.data(), hc.pp_exact.size()))) {
+            hss_close(h);
+            return s;
+        }
+        h->dev.limit = limit;
+        h->dev.spf = spf;
+        h->dev.seg_off = seg;
+        h->dev.hot = hot;
+        h->dev.exact = ex;
+        h->dev.owner = owner;
+        h->dev.pp_base = ppb;
+        h->dev.pp_hot = pph;
+        h->dev.pp_exact = ppx;
+        h->dev.max_exponent = hc.max_exponent;
+        h->seg_off = std::move(hc.seg_off);
+        h->spf = std::move(hc.spf);
+    }
+    uint8_t tables[kTableBytes];
+    build_residue_tables(tables);
+    h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
+    h->merged_cap = (uint32_t)kMergedCap;
+    if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
+        (s = device_alloc(h, &h->d_ctrl, 4)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
+        (s = ensure_rows(h, 1024))) {
+        hss_close(h);
+        return s;
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+        hss_close(h);
+        return HSS_ERR_CUDA;
+    }
+    *out = h;
+    return HSS_OK;
+}
+
+int hss_serve_stop(hss_t* h);
+
+void hss_close(hss_t* h) {
+    if (!h) return;
+    hss_serve_stop(h);
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void* p : h->allocations) cudaFree(p);
+    if (h->h_items) cudaFreeHost(h->h_items);
+    if (h->h_rows) cudaFreeHost(h->h_rows);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int hss_info(const hss_t* h, uint64_t* limit, uint64_t* records, uint64_t* flattened, uint64_t* cached,
+             double* prep_seconds) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    if (limit) *limit = h->limit;
+    if (records) *records = h->records;
+    if (flattened) *flattened = h->ref_flattened;
+    if (cached) *cached = h->ref_cached;
+    if (prep_seconds) *prep_seconds = h->prep_seconds;
+    return HSS_OK;
+}
+
+int hss_cache_inspect(uint64_t limit, uint64_t x, uint64_t* records, uint64_t* flattened, uint64_t* cached,
+                      int64_t* re, int64_t* im, uint32_t cap, uint32_t* count) {
+    if (limit < 1 || limit > HSS_MAX_LIMIT || x > limit) return HSS_ERR_ARGUMENT;
+    HostCache hc;
+    std::string err;
+    unsigned hw = std::thread::hardware_concurrency();
+    int s = build_host_cache(limit, (int)(hw ? hw : 1), &hc, &err);
+    if (s) return s;
+    if (records) *records = hc.records;
+    if (flattened) *flattened = hc.reference_flattened;
+    if (cached) *cached = hc.reference_cached;
+    if (x) {
+        uint32_t a = hc.seg_off[x], b = hc.seg_off[x + 1];
+        if (count) *count = b - a;
+        for (uint32_t i = a; i < b && i - a < cap; ++i) {
+            if (re) re[i - a] = hc.exact[i].re;
+            if (im) im[i - a] = hc.exact[i].im;
+        }
+    }
+    return HSS_OK;
+}
+
+int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* out, uint64_t* row_candidates,
+               hss_hit* hits, uint32_t hit_cap, uint32_t* nhits) {
+    if (!h || !out) return HSS_ERR_ARGUMENT;
+    if (first < 1 || first > last || last > h->limit)
+        return fail(h, HSS_ERR_ARGUMENT, "need 1 <= first <= last <= limit");
+    if (mode != HSS_MODE_PLAIN && mode != HSS_MODE_BATCHED) return fail(h, HSS_ERR_ARGUMENT, "unknown mode");
+    std::lock_guard<std::mutex> lock(h->gpu_mu);
+    HSS_CUDA(h, cudaSetDevice(h->device));
+    const size_t rows = (size_t)(last - first + 1);
+    int s = begin_call(h, rows);
+    if (s) return s;
+    if (mode == HSS_MODE_PLAIN) {
+        s = run_plain(h, first, last);
+    } else {
+        std::vector<RowRef> refs(rows);
+        for (size_t r = 0; r < rows; ++r) refs[r] = RowRef{first + r, (uint32_t)r};
+        s = run_batched(h, refs);
+    }
+    if (s) return s;
+    std::vector<DevHit> found;
+    uint32_t nfound = 0;
+    double ms = 0;
+    if ((s = end_call(h, rows, &ms, &found, &nfound))) return s;
+    memset(out, 0, sizeof *out);
+    for (size_t r = 0; r < rows; ++r) {
+        add_row(out, h->h_rows[r]);
+        out->pairs += h->limit - (first + r) + 1;
+        if (row_candidates) row_candidates[r] = h->h_rows[r].candidates;
+    }
+    out->hits = nfound;
+    out->kernel_ms = ms;
+    if (hits) copy_hits(found, hits, hit_cap);
+    if (nhits) *nhits = nfound;
+    return HSS_OK;
+}
+
+int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uint32_t count,
+                    hss_counts* per_interval, hss_counts* total, hss_hit* hits, uint32_t hit_cap,
+                    uint32_t* nhits) {
+    if (!h || !firsts || !lasts || count == 0) return HSS_ERR_ARGUMENT;
+    size_t rows = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        if (firsts[i] < 1 || firsts[i] > lasts[i] || lasts[i] > h->limit)
+            return fail(h, HSS_ERR_ARGUMENT, "need 1 <= first <= last <= limit for every interval");
+        rows += lasts[i] - firsts[i] + 1;
+    }
+    if (rows > UINT32_MAX) return fail(h, HSS_ERR_ARGUMENT, "too many rows");
+    std::lock_guard<std::mutex> lock(h->gpu_mu);
+    HSS_CUDA(h, cudaSetDevice(h->device));
+    int s = begin_call(h, rows);
+    if (s) return s;
+    std::vector<RowRef> refs;
+    refs.reserve(rows);
+    for (uint32_t i = 0; i < count; ++i)
+        for (uint64_t l = firsts[i]; l <= lasts[i]; ++l) refs.push_back(RowRef{l, (uint32_t)refs.size()});
+    if ((s = run_batched(h, refs))) return s;
+    std::vector<DevHit> found;
+    uint32_t nfound = 0;
+    double ms = 0;
+    if ((s = end_call(h, rows, &ms, &found, &nfound))) return s;
+    hss_counts sum{};
+    size_t r = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        hss_counts c{};
+        for (uint64_t l = firsts[i]; l <= lasts[i]; ++l, ++r) {
+            add_row(&c, h->h_rows[r]);
+            c.pairs += h->limit - l + 1;
+        }
+        for (const DevHit& hit : found)
+            if (hit.l >= firsts[i] && hit.l <= lasts[i]) ++c.hits;
+        if (per_interval) per_interval[i] = c;
+        sum.pairs += c.pairs;
+        sum.processed += c.processed;
+        sum.products += c.products;
+        sum.candidates += c.candidates;
+        sum.r16 += c.r16;
+        sum.exact += c.exact;
+        sum.merged += c.merged;
+    }
+    sum.hits = nfound;
+    sum.kernel_ms = ms;
+    if (total) *total = sum;
+    if (hits) copy_hits(found, hits, hit_cap);
+    if (nhits) *nhits = nfound;
+    return HSS_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------ serving
+
+namespace {
+
+struct Request {
+    uint64_t id = 0, first = 0, last = 0;
+    uint64_t next_row = 0;  // next root to schedule
+    uint64_t rows_done = 0;
+    uint64_t submitted_ns = 0, admitted_ns = 0, finished_ns = 0;
+    hss_counts counts{};
+    std::vector<DevHit> hits;
+    int status = HSS_ERR_BUSY;
+    bool admitted = false;
+};
+
+// One wave: a slice of every admitted request, run as one batched launch
+// sequence; row counters and hits are attributed back by row index.
+void serve_loop(hss_t* h) {
+    cudaSetDevice(h->device);
+    std::vector<Request*> active;
+    for (;;) {
+        std::vector<RowRef> rows;
+        std::vector<Request*> owner;
+        {
+            std::unique_lock<std::mutex> lock(h->serve_mu);
+            h->serve_cv.wait(lock, [&] { return h->serve_stop || !h->pending.empty() || !active.empty(); });
+            if (h->serve_stop) break;
+            // admission: request slots and free device memory (row counters,
+            // items and hits of its share of a wave)
+            while (!h->pending.empty() && active.size() < h->max_active) {
+                Request* r = h->requests[h->pending.front()];
+                size_t free_b = 0, total_b = 0;
+                cudaMemGetInfo(&free_b, &total_b);
+                size_t need = (size_t)(r->last - r->first + 1) * sizeof(RowCounts) + (64u << 20);
+                if (free_b < need && !active.empty()) break;
+                h->pending.pop_front();
+                r->admitted = true;
+                r->admitted_ns = now_ns();
+                r->next_row = r->first;
+                active.push_back(r);
+            }
+            const uint64_t budget = (uint64_t)h->wave_items << 20;
+            const uint64_t share = std::max<uint64_t>(budget / std::max<size_t>(active.size(), 1), 1);
+            for (Request* r : active) {
+                uint64_t taken = 0;
+                while (r->next_row <= r->last && (taken == 0 || taken + (h->limit - r->next_row + 1) <= share)) {
+                    taken += h->limit - r->next_row + 1;
+                    rows.push_back(RowRef{r->next_row, (uint32_t)rows.size()});
+                    owner.push_back(r);
+                    ++r->next_row;
+                }
+            }
+        }
+        std::vector<DevHit> found;
+        uint32_t nfound = 0;
+        double ms = 0;
+        int s;
+        {
+            std::lock_guard<std::mutex> g(h->gpu_mu);
+            s = begin_call(h, rows.size());
+            if (!s) s = run_batched(h, rows);
+            if (!s) s = end_call(h, rows.size(), &ms, &found, &nfound);
+        }
+        std::lock_guard<std::mutex> lock(h->serve_mu);
+        for (size_t i = 0; i < rows.size(); ++i) {
+            Request* r = owner[i];
+            if (s) {
+                r->status = s;
+                continue;
+            }
+            add_row(&r->counts, h->h_rows[i]);
+            r->counts.pairs += h->limit - rows[i].l + 1;
+            r->counts.kernel_ms += ms * (double)(h->limit - rows[i].l + 1);  // pair-weighted share, normalised below
+            ++r->rows_done;
+        }
+        for (const DevHit& hit : found)
+            if (hit.row < owner.size()) owner[hit.row]->hits.push_back(hit);
+        uint64_t t = now_ns();
+        for (size_t i = 0; i < active.size();) {
+            Request* r = active[i];
+            bool done = r->status != HSS_ERR_BUSY || r->rows_done == r->last - r->first + 1;
+            if (done) {
+                if (r->status == HSS_ERR_BUSY) r->status = HSS_OK;
+                r->finished_ns = t;
+                r->counts.kernel_ms /= (double)std::max<uint64_t>(r->counts.pairs, 1);
+                r->counts.hits = r->hits.size();
+                active[i] = active.back();
+                active.pop_back();
+            } else {
+                ++i;
+            }
+        }
+        h->serve_cv.notify_all();
+    }
+}
+
+int request_info(hss_t* h, Request* r, hss_request_info* info, hss_hit* hits, uint32_t cap) {
+    if (info) {
+        info->first = r->first;
+        info->last = r->last;
+        info->submitted_ns = r->submitted_ns;
+        info->admitted_ns = r->admitted_ns;
+        info->finished_ns = r->finished_ns;
+        info->counts = r->counts;
+        info->nhits = (uint32_t)r->hits.size();
+        info->status = r->status;
+    }
+    if (hits && r->status == HSS_OK) copy_hits(r->hits, hits, cap);
+    (void)h;
+    return r->status == HSS_ERR_BUSY ? HSS_ERR_BUSY : HSS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hss_serve_start(hss_t* h, uint32_t max_active, uint32_t wave_mpairs) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lock(h->serve_mu);
+    if (h->serving) return HSS_OK;
+    h->max_active = max_active ? max_active : 64;
+    h->wave_items = wave_mpairs ? wave_mpairs : 256;
+    h->serve_stop = false;
+    h->serving = true;
+    h->serve_thread = std::thread(serve_loop, h);
+    return HSS_OK;
+}
+
+int hss_submit(hss_t* h, uint64_t first, uint64_t last, uint64_t* request_id) {
+    if (!h || !request_id) return HSS_ERR_ARGUMENT;
+    if (first < 1 || first > last || last > h->limit) return fail(h, HSS_ERR_ARGUMENT, "need 1 <= first <= last <= limit");
+    std::lock_guard<std::mutex> lock(h->serve_mu);
+    if (!h->serving) return fail(h, HSS_ERR_ARGUMENT, "serving loop not started");
+    Request* r = new Request();
+    r->id = h->next_id++;
+    r->first = first;
+    r->last = last;
+    r->submitted_ns = now_ns();
+    h->requests[r->id] = r;
+    h->pending.push_back(r->id);
+    *request_id = r->id;
+    h->serve_cv.notify_all();
+    return HSS_OK;
+}
+
+int hss_poll(hss_t* h, uint64_t request_id, hss_request_info* info, hss_hit* hits, uint32_t hit_cap) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> lock(h->serve_mu);
+    auto it = h->requests.find(request_id);
+    if (it == h->requests.end()) return HSS_ERR_NOT_FOUND;
+    return request_info(h, it->second, info, hits, hit_cap);
+}
+
+int hss_wait(hss_t* h, uint64_t request_id, hss_request_info* info, hss_hit* hits, uint32_t hit_cap) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    std::unique_lock<std::mutex> lock(h->serve_mu);
+    auto it = h->requests.find(request_id);
+    if (it == h->requests.end()) return HSS_ERR_NOT_FOUND;
+    Request* r = it->second;
+    h->serve_cv.wait(lock, [&] { return r->status != HSS_ERR_BUSY || h->serve_stop; });
+    return request_info(h, r, info, hits, hit_cap);
+}
+
+int hss_serve_stop(hss_t* h) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    {
+        std::lock_guard<std::mutex> lock(h->serve_mu);
+        if (!h->serving) return HSS_OK;
+        h->serve_stop = true;
+        h->serve_cv.notify_all();
+    }
+    if (h->serve_thread.joinable()) h->serve_thread.join();
+    std::lock_guard<std::mutex> lock(h->serve_mu);
+    for (auto& kv : h->requests) delete kv.second;
+    h->requests.clear();
+    h->pending.clear();
+    h->serving = false;
+    return HSS_OK;
+}
+
+}  // extern "C"

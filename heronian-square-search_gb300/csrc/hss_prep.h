@@ -1,0 +1,48 @@
+// hss_prep.h - host-side construction of the factor cache for one limit N.
+#pragma once
+#include <stdint.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "hss_internal.h"
+
+namespace hss {
+
+// Per-integer factor summary used on the host (and by the item builder).
+struct NumberFactors {
+    uint32_t primes[8];   // distinct split primes p = 1 (mod 4), increasing
+    uint8_t exps[8];
+    uint8_t count;
+    uint64_t fixed;       // prod over p = 2 or p = 3 (mod 4) of p^(2a)
+};
+
+struct HostCache {
+    uint64_t limit = 0;
+    uint64_t records = 0;                 // total hot/exact records
+    std::vector<uint32_t> spf;            // [N+1]
+    std::vector<uint32_t> seg_off;        // [N+2]
+    std::unique_ptr<HotRec[]> hot;        // [records]
+    std::unique_ptr<ExactRec[]> exact;    // [records]
+    std::unique_ptr<uint32_t[]> owner;    // [records]
+    std::vector<uint32_t> pp_base;        // [N+1], UINT32_MAX if p is not a split prime
+    std::vector<HotRec> pp_hot;           // prime-power values (hot)
+    std::vector<__int128> pp_exact;       // prime-power values (re, im interleaved)
+    uint32_t max_exponent = 0;
+    // Sizes the reference's own preparation reports on stderr, recomputed for
+    // this cache: "flattened N Gaussian values" (gpu_search_v42.cu:606) and
+    // "cached N Gaussian pair values" (gpu_search_v42.cu:567).
+    uint64_t reference_flattened = 0;
+    uint64_t reference_cached = 0;
+    double seconds = 0;
+};
+
+// Builds the cache for limit N with up to `threads` host threads.  Returns 0
+// on success or a negative hss status with a message in *err.
+int build_host_cache(uint64_t limit, int threads, HostCache* out, std::string* err);
+
+// Factor summary of x from the smallest-prime-factor table.
+NumberFactors factor_number(const uint32_t* spf, uint64_t x);
+
+}  // namespace hss

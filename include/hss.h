@@ -1,0 +1,169 @@
+/*
+ * hss.h - C ABI of the GB300 (sm_103a) square-sided Heronian triangle search.
+ *
+ * The reference has no library interface: its GPU search is one CUDA program
+ * whose kernel signature and host object are the in-process boundary
+ * (src/gpu_search_v42.cu:292-297 `search_kernel(n, first_l, info, fourth,
+ * has_inert, prime_offsets, values, factor_info, cached, hits, hit_count,
+ * candidate_total)`, owned by `Search::prepare` :354 and `Search::run` :393),
+ * and its process boundary is the command line `gpu_search_v42 LIMIT FIRST_L
+ * LAST_L RESULTS_FILE [GPU [STATE_FILE]]` (:610-632).  This header replaces
+ * the in-process boundary; the command-line drop-in (gpu_search_v42) is built
+ * on top of it.
+ *
+ * Conventions: plain C types, caller-owned output buffers, opaque handles,
+ * status 0 on success and a negative HSS_ERR_* code on failure (message via
+ * hss_last_error).  A handle is not thread-safe; the serving calls are
+ * serialised internally.
+ */
+#ifndef HSS_H
+#define HSS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HSS_OK 0
+#define HSS_ERR_ARGUMENT (-1)  /* invalid argument (range, null pointer) */
+#define HSS_ERR_CUDA (-2)      /* CUDA runtime error (message has the detail) */
+#define HSS_ERR_MEMORY (-3)    /* host or device allocation failed */
+#define HSS_ERR_LIMIT (-4)     /* limit beyond what the cache layout indexes */
+#define HSS_ERR_STATE (-5)     /* checkpoint does not match the request */
+#define HSS_ERR_OVERFLOW (-6)  /* an internal capacity was exceeded */
+#define HSS_ERR_NOT_FOUND (-7) /* unknown request id */
+#define HSS_ERR_BUSY (-8)      /* request still running */
+#define HSS_ERR_NO_DEVICE (-9) /* no CUDA device / wrong architecture */
+
+#define HSS_MAX_LIMIT 100000000ULL
+
+/* Enumeration paths.  PLAIN mirrors the reference's launch shape (one block
+ * per (root, slice), one thread per pair, gpu_search_v42.cu:298-304);
+ * BATCHED is the persistent kernel draining a work queue of (root, m-range)
+ * items weighted by Gaussian divisor count.  Both give identical counts. */
+#define HSS_MODE_PLAIN 0
+#define HSS_MODE_BATCHED 1
+
+typedef struct hss_ctx hss_t;
+
+typedef struct {
+    uint32_t prep_threads;    /* host threads for the cache build (0: all cores) */
+    uint32_t hit_capacity;    /* device hit buffer per launch (0: 4096, as
+                                 gpu_search_v42.cu:177-178) */
+    uint32_t block_threads;   /* batched CTA size: 128, 256 or 512 (0: 256) */
+    uint32_t item_target;     /* batched item weight in alpha*beta evaluations
+                                 (0: 1<<20) */
+    uint32_t ctas_per_sm;     /* persistent CTAs per SM (0: from occupancy) */
+    uint32_t use_graph;       /* 1: capture each batched launch sequence in a
+                                 CUDA graph */
+} hss_opts;
+
+/* Counters of one search call.  `pairs` and `candidates` are the reference's
+ * counters (search_v18.cpp:322, gpu_search_v42.cu:160); the rest are the
+ * work figures the kernels export: processed pairs (not both even, no
+ * shared p = 3 mod 4 prime, some split prime), Gaussian products tested,
+ * candidates whose z = l^4+m^4-D passes mod 16, products settled by the
+ * exact 128-bit path, pairs sharing a split prime, and hits found. */
+typedef struct {
+    uint64_t pairs;
+    uint64_t processed;
+    uint64_t products;
+    uint64_t candidates;
+    uint64_t r16;
+    uint64_t exact;
+    uint64_t merged;
+    uint64_t hits;
+    double kernel_ms;  /* device time of the call's launches (CUDA events) */
+} hss_counts;
+
+/* A hit (l <= m <= n, gcd 1), with the signed 4A of the representation that
+ * produced it; area = |4A| / 4.  heron_ok is the device's 256-bit Heron
+ * recheck (all four Heron factors positive, product equal to (4A)^2). */
+typedef struct {
+    uint64_t l, m, n;
+    uint64_t area4_lo;
+    int64_t area4_hi;
+    uint32_t heron_ok;
+    uint32_t reserved;
+} hss_hit;
+
+/* Version string of the library. */
+const char* hss_version(void);
+
+/* Text for a status code. */
+const char* hss_strerror(int status);
+
+/* Last error message recorded on the handle (never NULL). */
+const char* hss_last_error(const hss_t* h);
+
+/* Builds the Gaussian factor cache for LIMIT on the host and makes it
+ * resident on `device` (replaces Search::prepare and the uploads of
+ * Search::run, gpu_search_v42.cu:354-432).  1 <= limit <= HSS_MAX_LIMIT. */
+int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out);
+
+/* Releases the device cache and the handle (gpu_search_v42.cu:496-505). */
+void hss_close(hss_t* h);
+
+/* Limit of the handle and sizes of its cache: records (free + central
+ * values), and the sizes the reference's preparation prints on stderr,
+ * "flattened N Gaussian values" and "cached N Gaussian pair values"
+ * (gpu_search_v42.cu:606, 567), recomputed for this limit. */
+int hss_info(const hss_t* h, uint64_t* limit, uint64_t* records, uint64_t* flattened,
+             uint64_t* cached, double* prep_seconds);
+
+/* Host-only inspection of the factor cache layout for LIMIT (no device is
+ * touched): the number of records (free + central values) and the two sizes
+ * the reference's preparation reports.  If x != 0, the segment of x (its free
+ * set followed by the central value x^2) is copied to re/im (up to cap
+ * values) and its length stored in *count. */
+int hss_cache_inspect(uint64_t limit, uint64_t x, uint64_t* records, uint64_t* flattened,
+                      uint64_t* cached, int64_t* re, int64_t* im, uint32_t cap, uint32_t* count);
+
+/* Searches root rows first..last (1 <= first <= last <= limit) against all
+ * m in [l, limit] with the given mode (one reference "batch" when last-first
+ * < 512, gpu_search_v42.cu:456-482).  Counters go to *out.  row_candidates,
+ * if not NULL, receives last-first+1 per-row candidate counts.  Up to
+ * hit_cap hits are copied to `hits`, sorted by (l, m, n) and deduplicated;
+ * *nhits receives the number found (which may exceed hit_cap). */
+int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* out,
+               uint64_t* row_candidates, hss_hit* hits, uint32_t hit_cap, uint32_t* nhits);
+
+/* Batched search of several intervals in one persistent launch sequence:
+ * intervals i = [firsts[i], lasts[i]].  per_interval (count entries) receives
+ * each interval's counters; hits of all intervals are returned together. */
+int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uint32_t count,
+                    hss_counts* per_interval, hss_counts* total, hss_hit* hits,
+                    uint32_t hit_cap, uint32_t* nhits);
+
+/* ---- serving: continuous admission of interval requests ----
+ * Requests are queued by hss_submit and advanced by a background loop that
+ * launches waves of batched work; each wave takes a bounded slice of every
+ * admitted request, so requests that arrive while others run join at the
+ * next wave.  Admission is capped by free device memory and by
+ * max_active.  Results are the same as hss_search on the same interval. */
+typedef struct {
+    uint64_t first, last;
+    uint64_t submitted_ns;  /* CLOCK_MONOTONIC at submit */
+    uint64_t admitted_ns;   /* when the request first joined a wave */
+    uint64_t finished_ns;   /* when its last wave completed (0 if running) */
+    hss_counts counts;
+    uint32_t nhits;
+    int32_t status;         /* HSS_OK when done, HSS_ERR_BUSY while running */
+} hss_request_info;
+
+/* max_active: requests admitted at once (0: 64).  wave_mpairs: logical pairs
+ * per wave in units of 2^20 (0: 256), shared among the admitted requests. */
+int hss_serve_start(hss_t* h, uint32_t max_active, uint32_t wave_mpairs);
+int hss_submit(hss_t* h, uint64_t first, uint64_t last, uint64_t* request_id);
+int hss_poll(hss_t* h, uint64_t request_id, hss_request_info* info, hss_hit* hits,
+             uint32_t hit_cap);
+int hss_wait(hss_t* h, uint64_t request_id, hss_request_info* info, hss_hit* hits,
+             uint32_t hit_cap);
+int hss_serve_stop(hss_t* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HSS_H */

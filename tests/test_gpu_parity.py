@@ -1,0 +1,136 @@
+"""Parity of the sm_103a kernels (through the C ABI) with the reference.
+
+Bit-exact integer work: candidate counts, logical pairs and hits must equal
+the reference's; processed pairs, products and mod-16 survivors must equal
+the oracle's.  Small cases compare per root row with the CPU oracle; the
+reference's own golden runs and published counts are checked at full size,
+including one whole reference batch at LIMIT 10^7.
+"""
+import random
+
+import pytest
+
+import hss
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("pairs", "processed", "products", "candidates", "r16")
+
+
+@pytest.fixture(scope="module")
+def searches(built):
+    cache = {}
+
+    def get(limit):
+        if limit not in cache:
+            cache[limit] = hss.Search(limit)
+        return cache[limit]
+
+    yield get
+    for s in cache.values():
+        s.close()
+
+
+def lines(hits):
+    return [f"{l} {m} {n} {a}" for l, m, n, a in hits]
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain"])
+@pytest.mark.parametrize("limit,first,last", [(200, 1, 200), (1000, 1, 1000), (3000, 1100, 1300),
+                                              (20000, 5500, 5530), (100000, 32040, 32050)])
+def test_rows_match_oracle(searches, mode, limit, first, last):
+    with Oracle(limit) as o:
+        want = o.search(first, last)
+    got = searches(limit).search(first, last, mode=mode, rows=True)
+    for key in FIELDS:
+        assert got.counts[key] == want[key], key
+    assert got.row_candidates == want["row_candidates"]
+    assert sorted(got.hits) == sorted(want["hits"])
+
+
+@pytest.mark.parametrize("mode", ["batched", "plain"])
+def test_smoke_cases(searches, published, mode):
+    for case in published["cases"]:
+        if case["name"] not in ("full5000", "known2"):
+            continue
+        r = searches(case["limit"]).search(case["first"], case["last"], mode=mode)
+        assert r.counts["pairs"] == case["pairs"]
+        assert r.counts["candidates"] == case["candidates"]
+        assert lines(r.hits) == case["results"]
+        assert all(r.heron_ok)
+
+
+def test_golden_reference_runs(searches, golden_runs):
+    for run in golden_runs:
+        r = searches(run["limit"]).search(run["first"], run["last"])
+        assert r.counts["pairs"] == run["pairs"], run
+        assert r.counts["candidates"] == run["candidates"], run
+        assert lines(r.hits) == run["results"], run
+
+
+def test_full100k_interval(searches, published):
+    """Root edges 1..100000: 5e9 logical pairs, both known solutions."""
+    case = next(c for c in published["cases"] if c["name"] == "full100k")
+    r = searches(case["limit"]).search(case["first"], case["last"])
+    assert r.counts["pairs"] == case["pairs"]
+    assert r.counts["candidates"] == case["candidates"]
+    assert lines(r.hits) == case["results"]
+    assert all(r.heron_ok)
+
+
+@pytest.mark.parametrize("name", ["reference_interval", "v45_ab_interval", "cpu_v18_500000",
+                                  "cpu_v18_1160000"])
+def test_production_limit_pins(searches, published, name):
+    case = next(c for c in published["cases"] if c["name"] == name)
+    r = searches(case["limit"]).search(case["first"], case["last"])
+    if "pairs" in case:
+        assert r.counts["pairs"] == case["pairs"]
+    assert r.counts["candidates"] == case["candidates"]
+    assert lines(r.hits) == case["results"]
+
+
+def test_plain_equals_batched_at_production_limit(searches):
+    s = searches(10 ** 7)
+    a = s.search(7500000, 7500063, mode="plain", rows=True)
+    b = s.search(7500000, 7500063, mode="batched", rows=True)
+    for key in FIELDS:
+        assert a.counts[key] == b.counts[key]
+    assert a.row_candidates == b.row_candidates
+
+
+def test_search_many_equals_single_intervals(searches):
+    """Uneven intervals in one persistent launch (the batched workload shape):
+    per-interval counts equal separate searches."""
+    rng = random.Random(7)
+    s = searches(100000)
+    intervals = []
+    for _ in range(24):
+        length = int(2 ** rng.uniform(0, 6))
+        start = rng.randint(1, 100000 - length)
+        intervals.append((start, start + length - 1))
+    per, total = s.search_many(intervals)
+    for (a, b), counts in zip(intervals, per):
+        single = s.search(a, b)
+        for key in FIELDS:
+            assert counts[key] == single.counts[key], (a, b, key)
+    assert total.counts["candidates"] == sum(p["candidates"] for p in per)
+
+
+def test_serving_results_same_alone_and_in_mix(searches):
+    """Requests admitted while others run give the counts they give alone."""
+    s = searches(100000)
+    reqs = [(1, 2000), (11789, 11789), (50000, 50400), (99000, 99999), (32045, 32045), (1800, 1900)]
+    alone = [s.search(a, b) for a, b in reqs]
+    s.serve_start(max_active=4, wave_mpairs=16)
+    try:
+        ids = [s.submit(a, b) for a, b in reqs]
+        done = [s.wait(i) for i in ids]
+    finally:
+        s.serve_stop()
+    for want, got in zip(alone, done):
+        assert got["status"] == 0
+        for key in FIELDS:
+            assert got["counts"][key] == want.counts[key], key
+        assert sorted(got["hits"]) == sorted(want.hits)
+        assert got["finished_ns"] >= got["admitted_ns"] >= got["submitted_ns"]
