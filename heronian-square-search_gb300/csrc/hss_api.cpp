@@ -14,6 +14,7 @@
 #include <time.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <condition_variable>
 #include <deque>
@@ -66,7 +67,9 @@ struct hss_ctx {
     size_t rows_cap = 0;
     DevHit* d_hits = nullptr;
     uint32_t hit_cap = 0;
-    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags
+    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count
+    uint4* d_big = nullptr;          // shared-prime pairs too big for a warp
+    uint32_t big_cap = 0;
     uint4* d_merged = nullptr;
     uint32_t merged_cap = 0;
     uint8_t* d_tables = nullptr;
@@ -78,6 +81,14 @@ struct hss_ctx {
     size_t h_rows_cap = 0;
 
     std::mutex gpu_mu;  // serialises device work on the handle
+
+    // per-call accounting: event triples (before main kernel, after it,
+    // after the shared-prime kernels) for every launch group
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    std::vector<std::array<cudaEvent_t, 3>> marks;
+    uint32_t launches = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
 
     // serving
     std::mutex serve_mu;
@@ -179,6 +190,21 @@ int ensure_rows(hss_t* h, size_t rows) {
     return HSS_OK;
 }
 
+// Grows the shared-prime queue (entries of 16 bytes) to hold `n` pairs.
+int ensure_merged(hss_t* h, uint64_t n) {
+    if (n <= h->merged_cap) return HSS_OK;
+    if (n >= UINT32_MAX) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue beyond 32-bit indexing");
+    HSS_CUDA(h, cudaStreamSynchronize(h->stream));
+    device_free(h, h->d_merged);
+    h->d_merged = nullptr;
+    uint64_t cap = n + n / 8;
+    if (cap >= UINT32_MAX) cap = UINT32_MAX - 1;
+    int s = device_alloc(h, &h->d_merged, (size_t)cap);
+    if (s) return s;
+    h->merged_cap = (uint32_t)cap;
+    return HSS_OK;
+}
+
 int ensure_items(hss_t* h, size_t n) {
     if (n > h->items_cap) {
         device_free(h, h->d_items);
@@ -210,7 +236,22 @@ LaunchBuffers buffers(const hss_t* h, size_t row_offset) {
     b.next_item = h->d_ctrl + 2;
     b.error_flags = h->d_ctrl + 3;
     b.tables = h->d_tables;
+    b.big_queue = h->d_big;
+    b.big_count = h->d_ctrl + 4;
+    b.big_cap = h->big_cap;
     return b;
+}
+
+int take_events(hss_t* h, std::array<cudaEvent_t, 3>* out) {
+    for (int i = 0; i < 3; ++i) {
+        if (h->events_used == h->event_pool.size()) {
+            cudaEvent_t e;
+            HSS_CUDA(h, cudaEventCreate(&e));
+            h->event_pool.push_back(e);
+        }
+        (*out)[i] = h->event_pool[h->events_used++];
+    }
+    return HSS_OK;
 }
 
 // A row of a launch: root l and its index in the call's row counters.
@@ -273,13 +314,17 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
 // fit the queue: reset cursor/queue, items H2D, persistent kernel, shared-prime
 // kernel.  Counters accumulate into d_rows[index].
 int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
+    // the pinned item buffer may still be read by the previous group's copy
+    HSS_CUDA(h, cudaStreamSynchronize(h->stream));
     uint32_t acap = 1, tcap = kTileMin;
     size_t n_items = build_items(h, rows, nrows, &acap, &tcap);
     if (n_items == (size_t)-1) return HSS_ERR_MEMORY;
     if (n_items == 0) return HSS_OK;
     HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                 h->stream));
+    h->h2d_bytes += n_items * sizeof(WorkItem);
     HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
+    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, sizeof(unsigned int), h->stream));
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
     cfg.alpha_cap = acap;
@@ -288,8 +333,15 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     int per_sm = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : batched_max_ctas_per_sm(cfg.threads, smem);
     cfg.ctas = h->sm_count * per_sm;
     LaunchBuffers b = buffers(h, 0);
+    std::array<cudaEvent_t, 3> ev;
+    if (int e = take_events(h, &ev)) return e;
+    HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
     HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
-    HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 8, h->stream));
+    HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
+    HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
+    HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    h->marks.push_back(ev);
+    h->launches += 3;
     return HSS_OK;
 }
 
@@ -322,11 +374,22 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
             bound += merged_bound(h, l);
             acap = std::max(acap, free_count(h, l) + 1);
         }
-        if (bound > h->merged_cap) return fail(h, HSS_ERR_OVERFLOW, "plain batch exceeds the shared-prime queue");
+        if (bound > h->merged_cap) {
+            int g = ensure_merged(h, bound);
+            if (g) return g;
+        }
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, sizeof(unsigned int), h->stream));
         LaunchBuffers buf = buffers(h, b - first);
+        std::array<cudaEvent_t, 3> ev;
+        if (int e = take_events(h, &ev)) return e;
+        HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
         HSS_CUDA(h, launch_plain(h->dev, b, nrows, acap, buf, h->stream));
-        HSS_CUDA(h, launch_merged(h->dev, 0, buf, h->sm_count * 8, h->stream));
+        HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, 0, buf, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
+        h->marks.push_back(ev);
+        h->launches += 3;
     }
     return HSS_OK;
 }
@@ -335,13 +398,18 @@ int begin_call(hss_t* h, size_t rows) {
     int s = ensure_rows(h, rows);
     if (s) return s;
     HSS_CUDA(h, cudaMemsetAsync(h->d_rows, 0, rows * sizeof(RowCounts), h->stream));
-    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl, 0, 4 * sizeof(unsigned int), h->stream));
+    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl, 0, 8 * sizeof(unsigned int), h->stream));
     HSS_CUDA(h, cudaEventRecord(h->ev0, h->stream));
+    h->events_used = 0;
+    h->marks.clear();
+    h->launches = 0;
+    h->h2d_bytes = h->d2h_bytes = 0;
     return HSS_OK;
 }
 
 // Copies row counters and hits back; hits sorted by (l, m, n) and deduplicated.
-int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint32_t* found) {
+int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint32_t* found,
+             double* main_ms = nullptr, double* merged_ms = nullptr) {
     HSS_CUDA(h, cudaEventRecord(h->ev1, h->stream));
     HSS_CUDA(h, cudaMemcpyAsync(h->h_rows, h->d_rows, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost,
                                 h->stream));
@@ -351,11 +419,23 @@ int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint3
     float f = 0;
     HSS_CUDA(h, cudaEventElapsedTime(&f, h->ev0, h->ev1));
     *ms = f;
+    double t_main = 0, t_merged = 0;
+    for (auto& ev : h->marks) {
+        float a = 0, b = 0;
+        HSS_CUDA(h, cudaEventElapsedTime(&a, ev[0], ev[1]));
+        HSS_CUDA(h, cudaEventElapsedTime(&b, ev[1], ev[2]));
+        t_main += a;
+        t_merged += b;
+    }
+    if (main_ms) *main_ms = t_main;
+    if (merged_ms) *merged_ms = t_merged;
+    h->d2h_bytes += rows * sizeof(RowCounts) + sizeof ctrl;
     if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
     if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
     uint32_t nh = std::min(ctrl[0], h->hit_cap);
     hits->resize(nh);
     if (nh) HSS_CUDA(h, cudaMemcpy(hits->data(), h->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
+    h->d2h_bytes += nh * sizeof(DevHit);
     std::sort(hits->begin(), hits->end(), [](const DevHit& a, const DevHit& b) {
         if (a.l != b.l) return a.l < b.l;
         if (a.m != b.m) return a.m < b.m;
@@ -375,6 +455,9 @@ void add_row(hss_counts* c, const RowCounts& r) {
     c->r16 += r.r16;
     c->exact += r.exact;
     c->merged += r.merged;
+    c->merged_products += r.mproducts;
+    c->merged_candidates += r.mcandidates;
+    c->merged_r16 += r.mr16;
 }
 
 void copy_hits(const std::vector<DevHit>& in, hss_hit* out, uint32_t cap) {
@@ -481,8 +564,10 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     build_residue_tables(tables);
     h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
     h->merged_cap = (uint32_t)kMergedCap;
+    h->big_cap = 1u << 20;
     if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
-        (s = device_alloc(h, &h->d_ctrl, 4)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
+        (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
+        (s = device_alloc(h, &h->d_big, h->big_cap)) ||
         (s = ensure_rows(h, 1024))) {
         hss_close(h);
         return s;
@@ -508,8 +593,19 @@ void hss_close(hss_t* h) {
     if (h->h_rows) cudaFreeHost(h->h_rows);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
+}
+
+int hss_int32_peak(int device, double* ops_per_second, double* ms) {
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return HSS_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return HSS_ERR_CUDA;
+    double v = int32_peak_ops(device, prop.multiProcessorCount, ms);
+    if (ops_per_second) *ops_per_second = v;
+    return v > 0 ? HSS_OK : HSS_ERR_CUDA;
 }
 
 int hss_info(const hss_t* h, uint64_t* limit, uint64_t* records, uint64_t* flattened, uint64_t* cached,
@@ -566,9 +662,14 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     if (s) return s;
     std::vector<DevHit> found;
     uint32_t nfound = 0;
-    double ms = 0;
-    if ((s = end_call(h, rows, &ms, &found, &nfound))) return s;
+    double ms = 0, main_ms = 0, merged_ms = 0;
+    if ((s = end_call(h, rows, &ms, &found, &nfound, &main_ms, &merged_ms))) return s;
     memset(out, 0, sizeof *out);
+    out->main_ms = main_ms;
+    out->merged_ms = merged_ms;
+    out->launches = h->launches;
+    out->h2d_bytes = h->h2d_bytes;
+    out->d2h_bytes = h->d2h_bytes;
     for (size_t r = 0; r < rows; ++r) {
         add_row(out, h->h_rows[r]);
         out->pairs += h->limit - (first + r) + 1;
@@ -603,9 +704,14 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
     if ((s = run_batched(h, refs))) return s;
     std::vector<DevHit> found;
     uint32_t nfound = 0;
-    double ms = 0;
-    if ((s = end_call(h, rows, &ms, &found, &nfound))) return s;
+    double ms = 0, main_ms = 0, merged_ms = 0;
+    if ((s = end_call(h, rows, &ms, &found, &nfound, &main_ms, &merged_ms))) return s;
     hss_counts sum{};
+    sum.main_ms = main_ms;
+    sum.merged_ms = merged_ms;
+    sum.launches = h->launches;
+    sum.h2d_bytes = h->h2d_bytes;
+    sum.d2h_bytes = h->d2h_bytes;
     size_t r = 0;
     for (uint32_t i = 0; i < count; ++i) {
         hss_counts c{};
@@ -623,6 +729,9 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
         sum.r16 += c.r16;
         sum.exact += c.exact;
         sum.merged += c.merged;
+        sum.merged_products += c.merged_products;
+        sum.merged_candidates += c.merged_candidates;
+        sum.merged_r16 += c.merged_r16;
     }
     sum.hits = nfound;
     sum.kernel_ms = ms;

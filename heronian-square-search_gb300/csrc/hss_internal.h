@@ -85,6 +85,10 @@ struct RowCounts {
     unsigned long long r16;         // candidates whose z passes mod 16 (R)
     unsigned long long exact;       // products resolved on the exact path
     unsigned long long merged;      // pairs that share a split prime
+    unsigned long long mproducts;   // products of those pairs (shared-prime kernels)
+    unsigned long long mcandidates;
+    unsigned long long mr16;
+    unsigned long long pad;
 };
 
 // A hit as produced on the device: roots and the signed 4A of the

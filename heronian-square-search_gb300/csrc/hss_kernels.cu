@@ -47,8 +47,11 @@ constexpr uint32_t kSqC = kModC * kModC;
 constexpr uint32_t kTabA = 0, kTabB = 720, kTabC = 720 + 625;
 constexpr uint32_t kSlices = 8;           // plain kernel: blocks per row
 constexpr uint32_t kPlainThreads = 128;   // plain kernel: threads per block
-constexpr uint32_t kMergedThreads = 128;
-constexpr uint32_t kMergedListCap = 2048; // alpha + beta entries per shared-prime pair
+constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
+constexpr uint32_t kMergedListCap = 2048;  // alpha + beta entries of one big pair
+constexpr uint32_t kWarpPairThreads = 256; // shared-prime pairs: one warp per pair
+constexpr uint32_t kWarpPairWarps = kWarpPairThreads / 32;
+constexpr uint32_t kWarpListCap = 192;     // alpha + beta entries of one warp's pair
 constexpr uint32_t kMaxTerms = 16;
 
 // Window and filter constants of one pair (l, m).
@@ -264,7 +267,7 @@ __device__ __noinline__ void resolve_exact(uint32_t st, i128 ar, i128 ai, i128 b
 
 // Deeper residue filters mod 625 and 1547 for a counted orientation whose z
 // passed the mod-720 table; true when some counted sign survives.
-__device__ __noinline__ bool deep_filters(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw,
+__device__ __forceinline__ bool deep_filters(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw,
                                              int k, int o, bool neg, bool c1, bool c2, uint32_t sres,
                                              bool flag5, const uint8_t* tab) {
     uint32_t ar = (arw >> 10) & 1023u, ai = (aiw >> 10) & 1023u, br = (brw >> 10) & 1023u,
@@ -492,7 +495,9 @@ __device__ __forceinline__ void push_merged(const LaunchBuffers& buf, uint32_t l
         atomicOr(buf.error_flags, 1u);
 }
 
-__device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc) {
+// Warp-level reduction of the per-thread counters into a row's counters;
+// `shared_prime` also books them as work of the shared-prime kernels.
+__device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc, bool shared_prime = false) {
     uint32_t v[6] = {acc.cand, acc.r16, acc.prod, acc.exact, acc.processed, acc.merged};
 #pragma unroll
     for (int i = 0; i < 6; ++i) v[i] = __reduce_add_sync(0xFFFFFFFFu, v[i]);
@@ -503,6 +508,11 @@ __device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc) {
         if (v[3]) atomicAdd(&rc->exact, (unsigned long long)v[3]);
         if (v[4]) atomicAdd(&rc->processed, (unsigned long long)v[4]);
         if (v[5]) atomicAdd(&rc->merged, (unsigned long long)v[5]);
+        if (shared_prime) {
+            if (v[0]) atomicAdd(&rc->mcandidates, (unsigned long long)v[0]);
+            if (v[1]) atomicAdd(&rc->mr16, (unsigned long long)v[1]);
+            if (v[2]) atomicAdd(&rc->mproducts, (unsigned long long)v[2]);
+        }
     }
     acc = Acc{0, 0, 0, 0, 0, 0};
 }
@@ -577,13 +587,37 @@ __global__ void __launch_bounds__(NT, 512 / NT) batched_kernel(const DeviceCache
             s_ctx[i] = c;
         }
         __syncthreads();
+        // Rounds of NT records: every lane runs the same alpha iteration at the
+        // same time (lanes without a record on this path are predicated off),
+        // so lanes never drift into different phases of the alpha loop.
         const uint32_t r0 = cache.seg_off[w.m0], r1 = cache.seg_off[w.m1];
-        for (uint32_t j = r0 + threadIdx.x; j < r1; j += NT) {
-            const uint32_t m = cache.owner[j];
-            const PairCtx c = s_ctx[m - w.m0];
-            if (!c.dinv) continue;
-            const HotRec b = cache.hot[j];
-            record_loop(s_alpha, na, b, c, s_tab, cache, a0, j, w.l, m, w.row, acc, buf);
+        for (uint32_t base = r0; base < r1; base += NT) {
+            const uint32_t j = base + threadIdx.x;
+            uint32_t m = 0;
+            PairCtx c;
+            c.dinv = 0;
+            HotRec b{0.f, 0.f, 0u, 0u};
+            if (j < r1) {
+                m = cache.owner[j];
+                c = s_ctx[m - w.m0];
+                b = cache.hot[j];
+            }
+            const bool live = c.dinv != 0;
+            const bool cb = (b.rre & kCentralBit) != 0;
+            for (uint32_t k = 0; k < na; ++k) {
+                const HotRec a = s_alpha[k];
+                const bool ca = (a.rre & kCentralBit) != 0;
+                if (live && !(ca & cb)) {
+                    const bool two = !(ca | cb);
+                    acc.prod += two ? 2u : 1u;
+                    uint32_t st = eval_pair(a, b, two, c, s_tab, acc);
+                    if (st) {
+                        ExactRec ea = cache.exact[a0 + k], eb = cache.exact[j];
+                        resolve_exact(st, 2 * (__int128)ea.re, 2 * (__int128)ea.im, (__int128)eb.re,
+                                      (__int128)eb.im, w.l, m, cache.limit, w.row, s_tab, acc, buf);
+                    }
+                }
+            }
         }
         flush_acc(acc, &buf.rows[w.row]);
     }
@@ -709,7 +743,7 @@ __device__ HotRec hot_of(i128 re, i128 im, bool central) {
     return h;
 }
 
-__device__ void merged_setup(const DeviceCache& cache, uint4 q, MergedShared& S) {
+__device__ void merged_setup(const DeviceCache& cache, uint4 q, MergedShared& S, uint32_t list_cap) {
     uint64_t l = q.x, m = q.y;
     S.l = l;
     S.m = m;
@@ -778,30 +812,30 @@ __device__ void merged_setup(const DeviceCache& cache, uint4 q, MergedShared& S)
     group_finish(S.g[1]);
     S.g[0].scale = fixed;
     S.g[1].scale = 1;
-    if (S.g[0].free_count + S.g[1].free_count + 2 > kMergedListCap) S.ok = 0;
+    if (S.g[0].free_count + S.g[1].free_count + 2 > list_cap) S.ok = 2;  // too big for this path
 }
 
-__global__ void __launch_bounds__(kMergedThreads, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+__global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
     __shared__ MergedShared S;
     __shared__ __align__(16) HotRec s_list[kMergedListCap];
     __shared__ uint8_t s_tab[kTableBytes];
     __shared__ RowConst s_row;
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
-    const uint32_t count = min(*buf.merged_count, buf.merged_cap);
+    const uint32_t count = min(*buf.big_count, buf.big_cap);
     for (uint32_t q = blockIdx.x; q < count; q += gridDim.x) {
         __syncthreads();
         if (threadIdx.x == 0) {
-            uint4 e = buf.merged_queue[q];
-            merged_setup(cache, e, S);
+            uint4 e = buf.big_queue[q];
+            merged_setup(cache, e, S, kMergedListCap);
             row_setup(cache, e.x, s_row);
             uint32_t cc_c, cc_r;
             S.ctx = make_ctx(s_row, e.y, cc_c, cc_r);
             S.cc_cand = cc_c;
             S.cc_r16 = cc_r;
-            if (!S.ok) atomicOr(buf.error_flags, 2u);
+            if (S.ok != 1) atomicOr(buf.error_flags, 2u);
         }
         __syncthreads();
-        if (!S.ok) continue;
+        if (S.ok != 1) continue;
         const uint32_t na = S.g[0].free_count + 1, nb = S.g[1].free_count + 1;
         HotRec* s_a = s_list;
         HotRec* s_b = s_list + na;
@@ -845,11 +879,146 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_kernel(const DeviceC
                 resolve_exact(st, ar, ai, br, bi, S.l, S.m, cache.limit, S.row, s_tab, acc, buf);
             }
         }
-        flush_acc(acc, &buf.rows[S.row]);
+        flush_acc(acc, &buf.rows[S.row], true);
     }
 }
 
+// Shared-prime pairs, one warp per pair: lane 0 factors the pair and splits
+// its terms, the lanes build both lists in the warp's shared slice, then all
+// (alpha, beta) combinations are evaluated in lockstep rounds of 32.  Pairs
+// whose lists exceed the slice go to the big-pair queue (one CTA per pair).
+__global__ void __launch_bounds__(kWarpPairThreads, 2) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+    __shared__ MergedShared S[kWarpPairWarps];
+    __shared__ RowConst R[kWarpPairWarps];
+    __shared__ __align__(16) HotRec s_list[kWarpPairWarps][kWarpListCap];
+    __shared__ uint8_t s_tab[kTableBytes];
+    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kWarpPairThreads) s_tab[i] = buf.tables[i];
+    __syncthreads();
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
+    MergedShared& P = S[warp];
+    HotRec* list = s_list[warp];
+    const uint32_t count = min(*buf.merged_count, buf.merged_cap);
+    const uint32_t stride = gridDim.x * kWarpPairWarps;
+    for (uint32_t q = blockIdx.x * kWarpPairWarps + warp; q < count; q += stride) {
+        __syncwarp();
+        if (lane == 0) {
+            uint4 e = buf.merged_queue[q];
+            merged_setup(cache, e, P, kWarpListCap);
+            if (P.ok == 1) {
+                row_setup(cache, e.x, R[warp]);
+                uint32_t cc_c, cc_r;
+                P.ctx = make_ctx(R[warp], e.y, cc_c, cc_r);
+                P.cc_cand = cc_c;
+                P.cc_r16 = cc_r;
+            } else if (P.ok == 2) {
+                unsigned int idx = atomicAdd(buf.big_count, 1u);
+                if (idx < buf.big_cap)
+                    buf.big_queue[idx] = e;
+                else
+                    atomicOr(buf.error_flags, 2u);
+            } else {
+                atomicOr(buf.error_flags, 2u);
+            }
+        }
+        __syncwarp();
+        if (P.ok != 1) continue;
+        const uint32_t na = P.g[0].free_count + 1, nb = P.g[1].free_count + 1;
+        for (uint32_t k = lane; k < na + nb; k += 32) {
+            int side = k < na ? 0 : 1;
+            uint32_t idx = side ? k - na : k;
+            __int128 re, im;
+            group_value(cache, P.g[side], idx, re, im);
+            list[k] = hot_of(re, im, idx == P.g[side].free_count);
+        }
+        __syncwarp();
+        Acc acc{0, 0, 0, 0, 0, 0};
+        if (lane == 0) {
+            acc.prod += 1;
+            acc.cand += P.cc_cand;
+            acc.r16 += P.cc_r16;
+        }
+        const PairCtx c = P.ctx;
+        const uint32_t total = na * nb;
+        const float rcp = 1.0f / (float)nb;
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t k = base + lane;
+            uint32_t ka = (uint32_t)((float)k * rcp);
+            int32_t kb = (int32_t)k - (int32_t)(ka * nb);
+            while (kb < 0) {
+                --ka;
+                kb += (int32_t)nb;
+            }
+            while (kb >= (int32_t)nb) {
+                ++ka;
+                kb -= (int32_t)nb;
+            }
+            if (k < total) {
+                const HotRec a = list[ka], b = list[na + kb];
+                const bool ca = (a.rre & kCentralBit) != 0, cb = (b.rre & kCentralBit) != 0;
+                if (!(ca & cb)) {
+                    const bool two = !(ca | cb);
+                    acc.prod += two ? 2u : 1u;
+                    uint32_t st = eval_pair(a, b, two, c, s_tab, acc);
+                    if (st) {
+                        __int128 ar, ai, br, bi;
+                        group_value(cache, P.g[0], ka, ar, ai);
+                        group_value(cache, P.g[1], (uint32_t)kb, br, bi);
+                        resolve_exact(st, ar, ai, br, bi, P.l, P.m, cache.limit, P.row, s_tab, acc, buf);
+                    }
+                }
+            }
+        }
+        flush_acc(acc, &buf.rows[P.row], true);
+    }
+}
+
+// INT32 throughput probe: 8 independent chains per thread, each step one
+// IMAD and one LOP3 (the multiply and logic pipes the search loop uses),
+// i.e. 16 integer instructions per unrolled step; the result is stored so
+// nothing is eliminated.
+__global__ void __launch_bounds__(256) int_peak_kernel(uint32_t iters, uint32_t seed, uint32_t* out) {
+    uint32_t a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = threadIdx.x * (i + 3) + blockIdx.x + seed;
+    for (uint32_t it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            a[i] = a[i] * 0x9E3779B1u + (uint32_t)i;
+            a[i] = (a[i] ^ (a[i] >> 7)) & 0x7FFFFFFFu;
+        }
+    }
+    uint32_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) r ^= a[i];
+    if (r == seed) out[0] = r;
+}
+
 }  // namespace
+
+double int32_peak_ops(int device, int sm_count, double* ms_out) {
+    cudaSetDevice(device);
+    uint32_t* out = nullptr;
+    if (cudaMalloc(&out, sizeof(uint32_t)) != cudaSuccess) return 0;
+    const int blocks = sm_count * 8, threads = 256;
+    const uint32_t iters = 1u << 14;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int_peak_kernel<<<blocks, threads>>>(64, 1, out);  // warm-up
+    cudaEventRecord(e0);
+    int_peak_kernel<<<blocks, threads>>>(iters, 1, out);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (ms_out) *ms_out = ms;
+    // per unrolled step: 8 IMAD + 8 shift-xor-and (SHF/LOP3 pairs count as 2)
+    double ops = (double)blocks * threads * iters * 8.0 * 3.0;
+    return ms > 0 ? ops / (ms * 1e-3) : 0;
+}
 
 // ------------------------------------------------------------------ host side
 
@@ -924,7 +1093,10 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf, int ctas,
                           cudaStream_t stream) {
     (void)count;
-    merged_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
+    merged_kernel<<<ctas, kWarpPairThreads, 0, stream>>>(cache, buf);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    merged_big_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
     return cudaGetLastError();
 }
 

@@ -25,7 +25,10 @@ struct LaunchBuffers {
     unsigned int* merged_count; // entries appended (may exceed merged_cap)
     uint32_t merged_cap;
     unsigned int* next_item;    // work-queue cursor of the batched kernel
-    unsigned int* error_flags;  // bit 0: merged list over capacity
+    unsigned int* error_flags;  // bit 0: shared-prime queue full; bit 1: pair lists over capacity
+    uint4* big_queue;           // shared-prime pairs too big for one warp's lists
+    unsigned int* big_count;
+    uint32_t big_cap;
     const uint8_t* tables;      // kTableBytes residue tables
 };
 
@@ -51,6 +54,9 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 // Pairs sharing a split prime, read from buf.merged_queue[0 .. count).
 cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf,
                           int ctas, cudaStream_t stream);
+
+// Integer-op throughput of the device measured by a probe kernel (ops/s).
+double int32_peak_ops(int device, int sm_count, double* ms);
 
 // Occupancy helper for the persistent grid.
 int batched_max_ctas_per_sm(int threads, size_t smem);

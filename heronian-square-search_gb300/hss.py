@@ -34,7 +34,12 @@ class HssCounts(ctypes.Structure):
     _fields_ = [("pairs", ctypes.c_uint64), ("processed", ctypes.c_uint64),
                 ("products", ctypes.c_uint64), ("candidates", ctypes.c_uint64),
                 ("r16", ctypes.c_uint64), ("exact", ctypes.c_uint64), ("merged", ctypes.c_uint64),
-                ("hits", ctypes.c_uint64), ("kernel_ms", ctypes.c_double)]
+                ("hits", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
+                ("main_ms", ctypes.c_double), ("merged_ms", ctypes.c_double),
+                ("merged_products", ctypes.c_uint64), ("merged_candidates", ctypes.c_uint64),
+                ("merged_r16", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64), ("launches", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -74,7 +74,16 @@ typedef struct {
     uint64_t exact;
     uint64_t merged;
     uint64_t hits;
-    double kernel_ms;  /* device time of the call's launches (CUDA events) */
+    double kernel_ms;   /* device time of the whole call (CUDA events on its stream) */
+    double main_ms;     /* device time of the batched / plain kernels */
+    double merged_ms;   /* device time of the shared-prime kernels */
+    uint64_t merged_products;    /* products, candidates and mod-16 survivors of */
+    uint64_t merged_candidates;  /* the pairs sharing a split prime (included in */
+    uint64_t merged_r16;         /* the totals above) */
+    uint64_t h2d_bytes;          /* host-to-device bytes copied by the call */
+    uint64_t d2h_bytes;          /* device-to-host bytes copied by the call */
+    uint32_t launches;           /* kernels launched by the call */
+    uint32_t reserved;
 } hss_counts;
 
 /* A hit (l <= m <= n, gcd 1), with the signed 4A of the representation that
@@ -111,6 +120,11 @@ void hss_close(hss_t* h);
  * (gpu_search_v42.cu:606, 567), recomputed for this limit. */
 int hss_info(const hss_t* h, uint64_t* limit, uint64_t* records, uint64_t* flattened,
              uint64_t* cached, double* prep_seconds);
+
+/* Measures the device's 32-bit integer instruction throughput with a probe
+ * kernel (independent multiply-add and shift/logic chains on every SM);
+ * used as the denominator of the integer roofline. */
+int hss_int32_peak(int device, double* ops_per_second, double* ms);
 
 /* Host-only inspection of the factor cache layout for LIMIT (no device is
  * touched): the number of records (free + central values) and the two sizes
