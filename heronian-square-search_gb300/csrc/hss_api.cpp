@@ -35,7 +35,7 @@ namespace {
 constexpr uint32_t kDefaultHitCap = 4096;      // gpu_search_v42.cu:177-178
 constexpr uint32_t kPlainBatch = 512;          // gpu_search_v42.cu:457
 constexpr uint32_t kDefaultItemTarget = 1u << 20;
-constexpr uint32_t kTileCap = 1024;            // largest m-range of one item
+constexpr uint32_t kTileCap = 8192;            // largest m-range of one item
 constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
 constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
@@ -67,9 +67,11 @@ struct hss_ctx {
     size_t rows_cap = 0;
     DevHit* d_hits = nullptr;
     uint32_t hit_cap = 0;
-    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count
+    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count [5] exact_count
     uint4* d_big = nullptr;          // shared-prime pairs too big for a warp
     uint32_t big_cap = 0;
+    ExactItem* d_exact = nullptr;    // exact work queue
+    uint32_t exact_cap = 0;
     uint4* d_merged = nullptr;
     uint32_t merged_cap = 0;
     uint8_t* d_tables = nullptr;
@@ -79,6 +81,9 @@ struct hss_ctx {
     size_t h_items_cap = 0;
     RowCounts* h_rows = nullptr;  // pinned
     size_t h_rows_cap = 0;
+    RowInfo* d_row_info = nullptr;  // constants of the call's rows
+    RowInfo* h_row_info = nullptr;  // pinned
+    size_t row_info_cap = 0;
 
     std::mutex gpu_mu;  // serialises device work on the handle
 
@@ -184,6 +189,7 @@ int ensure_rows(hss_t* h, size_t rows) {
     if (s) return s;
     h->rows_cap = cap;
     if (h->h_rows) cudaFreeHost(h->h_rows);
+    if (h->h_row_info) cudaFreeHost(h->h_row_info);
     h->h_rows = nullptr;
     HSS_CUDA(h, cudaMallocHost(&h->h_rows, cap * sizeof(RowCounts)));
     h->h_rows_cap = cap;
@@ -236,6 +242,10 @@ LaunchBuffers buffers(const hss_t* h, size_t row_offset) {
     b.next_item = h->d_ctrl + 2;
     b.error_flags = h->d_ctrl + 3;
     b.tables = h->d_tables;
+    b.row_info = h->d_row_info + row_offset;
+    b.exact_queue = h->d_exact;
+    b.exact_count = h->d_ctrl + 5;
+    b.exact_cap = h->exact_cap;
     b.big_queue = h->d_big;
     b.big_count = h->d_ctrl + 4;
     b.big_cap = h->big_cap;
@@ -264,12 +274,12 @@ struct RowRef {
 // about item_target alpha*beta evaluations (at most kTileCap roots), then
 // ordered by m so that concurrently running items read the same m-side
 // records from L2.  Returns the largest row segment and m-range.
-size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap, uint32_t* tile_cap) {
+size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap) {
     const uint64_t n = h->limit;
     const uint32_t target = h->opts.item_target ? h->opts.item_target : kDefaultItemTarget;
     std::vector<uint32_t> tile(nrows);
     size_t total = 0;
-    uint32_t acap = 1, tcap = kTileMin;
+    uint32_t acap = 1;
     for (size_t r = 0; r < nrows; ++r) {
         uint64_t l = rows[r].l;
         uint32_t na = free_count(h, l) + 1;
@@ -279,7 +289,6 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
         uint32_t tm = t >= kTileCap ? kTileCap : (uint32_t)t;
         tm = std::max(kTileMin, tm & ~(kTileMin - 1));
         tile[r] = tm;
-        tcap = std::max(tcap, tm);
         total += (n - l + 1 + tm - 1) / tm;
     }
     if (ensure_items(h, total)) return (size_t)-1;
@@ -298,8 +307,30 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
         }
     }
     *alpha_cap = acap;
-    *tile_cap = tcap;
     return total;
+}
+
+// Constants of the call's rows (row i of the call at index i).
+int upload_row_info(hss_t* h, const std::vector<uint64_t>& ls) {
+    if (ls.size() > h->row_info_cap) {
+        HSS_CUDA(h, cudaStreamSynchronize(h->stream));
+        device_free(h, h->d_row_info);
+        h->d_row_info = nullptr;
+        if (h->h_row_info) cudaFreeHost(h->h_row_info);
+        h->h_row_info = nullptr;
+        size_t cap = std::max(ls.size(), (size_t)1024);
+        int s = device_alloc(h, &h->d_row_info, cap);
+        if (s) return s;
+        HSS_CUDA(h, cudaMallocHost(&h->h_row_info, cap * sizeof(RowInfo)));
+        h->row_info_cap = cap;
+    }
+    HSS_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (size_t i = 0; i < ls.size(); ++i)
+        fill_row_info(h->spf.data(), h->seg_off.data(), h->limit, ls[i], &h->h_row_info[i]);
+    HSS_CUDA(h, cudaMemcpyAsync(h->d_row_info, h->h_row_info, ls.size() * sizeof(RowInfo), cudaMemcpyHostToDevice,
+                                h->stream));
+    h->h2d_bytes += ls.size() * sizeof(RowInfo);
+    return HSS_OK;
 }
 
 [[maybe_unused]] int check_errors(hss_t* h) {
@@ -316,21 +347,21 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
 int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     // the pinned item buffer may still be read by the previous group's copy
     HSS_CUDA(h, cudaStreamSynchronize(h->stream));
-    uint32_t acap = 1, tcap = kTileMin;
-    size_t n_items = build_items(h, rows, nrows, &acap, &tcap);
+    uint32_t acap = 1;
+    size_t n_items = build_items(h, rows, nrows, &acap);
     if (n_items == (size_t)-1) return HSS_ERR_MEMORY;
     if (n_items == 0) return HSS_OK;
     HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                 h->stream));
     h->h2d_bytes += n_items * sizeof(WorkItem);
     HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
-    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, sizeof(unsigned int), h->stream));
+    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
+    cfg.min_blocks = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 6 : cfg.threads == 512 ? 1 : 3);
     cfg.alpha_cap = acap;
-    cfg.tile_cap = tcap;
-    size_t smem = batched_smem_bytes(acap, tcap);
-    int per_sm = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : batched_max_ctas_per_sm(cfg.threads, smem);
+    size_t smem = batched_smem_bytes(cfg.threads, acap);
+    int per_sm = batched_max_ctas_per_sm(cfg.threads, cfg.min_blocks, smem);
     cfg.ctas = h->sm_count * per_sm;
     LaunchBuffers b = buffers(h, 0);
     std::array<cudaEvent_t, 3> ev;
@@ -339,9 +370,10 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
     HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
     HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
+    HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
     HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
     h->marks.push_back(ev);
-    h->launches += 3;
+    h->launches += 4;
     return HSS_OK;
 }
 
@@ -379,7 +411,7 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
             if (g) return g;
         }
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, sizeof(unsigned int), h->stream));
-        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
         LaunchBuffers buf = buffers(h, b - first);
         std::array<cudaEvent_t, 3> ev;
         if (int e = take_events(h, &ev)) return e;
@@ -387,9 +419,10 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
         HSS_CUDA(h, launch_plain(h->dev, b, nrows, acap, buf, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
         HSS_CUDA(h, launch_merged(h->dev, 0, buf, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, launch_exact(h->dev, buf, h->sm_count * 4, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
         h->marks.push_back(ev);
-        h->launches += 3;
+        h->launches += 4;
     }
     return HSS_OK;
 }
@@ -432,6 +465,7 @@ int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint3
     h->d2h_bytes += rows * sizeof(RowCounts) + sizeof ctrl;
     if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
     if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
+    if (ctrl[3] & 4u) return fail(h, HSS_ERR_OVERFLOW, "exact work queue over capacity");
     uint32_t nh = std::min(ctrl[0], h->hit_cap);
     hits->resize(nh);
     if (nh) HSS_CUDA(h, cudaMemcpy(hits->data(), h->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
@@ -529,6 +563,12 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
             delete h;
             return s;
         }
+        uint32_t longest = 0;
+        for (uint64_t x = 1; x <= limit; ++x) longest = std::max(longest, hc.seg_off[x + 1] - hc.seg_off[x]);
+        if (longest > kItemRecords) {
+            delete h;
+            return HSS_ERR_LIMIT;
+        }
         h->records = hc.records;
         h->ref_flattened = hc.reference_flattened;
         h->ref_cached = hc.reference_cached;
@@ -565,9 +605,10 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
     h->merged_cap = (uint32_t)kMergedCap;
     h->big_cap = 1u << 20;
+    h->exact_cap = 1u << 22;
     if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
         (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
-        (s = device_alloc(h, &h->d_big, h->big_cap)) ||
+        (s = device_alloc(h, &h->d_big, h->big_cap)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
         (s = ensure_rows(h, 1024))) {
         hss_close(h);
         return s;
@@ -591,6 +632,7 @@ void hss_close(hss_t* h) {
     for (void* p : h->allocations) cudaFree(p);
     if (h->h_items) cudaFreeHost(h->h_items);
     if (h->h_rows) cudaFreeHost(h->h_rows);
+    if (h->h_row_info) cudaFreeHost(h->h_row_info);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
@@ -652,6 +694,11 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     const size_t rows = (size_t)(last - first + 1);
     int s = begin_call(h, rows);
     if (s) return s;
+    {
+        std::vector<uint64_t> ls(rows);
+        for (size_t r = 0; r < rows; ++r) ls[r] = first + r;
+        if ((s = upload_row_info(h, ls))) return s;
+    }
     if (mode == HSS_MODE_PLAIN) {
         s = run_plain(h, first, last);
     } else {
@@ -682,6 +729,41 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     return HSS_OK;
 }
 
+int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tune_trial* trials,
+                 uint32_t max_trials, uint32_t* ntrials) {
+    if (!h) return HSS_ERR_ARGUMENT;
+    static const uint32_t kVariants[][2] = {{128, 4}, {128, 6}, {256, 2}, {256, 3}, {512, 1}};
+    static const uint32_t kTargets[] = {1u << 19, 1u << 20, 1u << 21};
+    const hss_opts saved = h->opts;
+    hss_opts chosen = saved;
+    float best_ms = 0;
+    uint32_t n = 0;
+    for (const auto& v : kVariants)
+        for (uint32_t target : kTargets) {
+            h->opts.block_threads = v[0];
+            h->opts.ctas_per_sm = v[1];
+            h->opts.item_target = target;
+            hss_counts c;
+            int s = hss_search(h, first, last, HSS_MODE_BATCHED, &c, nullptr, nullptr, 0, nullptr);  // warm
+            if (!s) s = hss_search(h, first, last, HSS_MODE_BATCHED, &c, nullptr, nullptr, 0, nullptr);
+            if (s) {
+                h->opts = saved;
+                return s;
+            }
+            float ms = (float)c.kernel_ms;
+            if (trials && n < max_trials) trials[n] = hss_tune_trial{v[0], v[1], target, ms};
+            ++n;
+            if (best_ms == 0 || ms < best_ms) {
+                best_ms = ms;
+                chosen = h->opts;
+            }
+        }
+    h->opts = chosen;
+    if (best) *best = chosen;
+    if (ntrials) *ntrials = n;
+    return HSS_OK;
+}
+
 int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uint32_t count,
                     hss_counts* per_interval, hss_counts* total, hss_hit* hits, uint32_t hit_cap,
                     uint32_t* nhits) {
@@ -698,9 +780,15 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
     int s = begin_call(h, rows);
     if (s) return s;
     std::vector<RowRef> refs;
+    std::vector<uint64_t> ls;
     refs.reserve(rows);
+    ls.reserve(rows);
     for (uint32_t i = 0; i < count; ++i)
-        for (uint64_t l = firsts[i]; l <= lasts[i]; ++l) refs.push_back(RowRef{l, (uint32_t)refs.size()});
+        for (uint64_t l = firsts[i]; l <= lasts[i]; ++l) {
+            refs.push_back(RowRef{l, (uint32_t)refs.size()});
+            ls.push_back(l);
+        }
+    if ((s = upload_row_info(h, ls))) return s;
     if ((s = run_batched(h, refs))) return s;
     std::vector<DevHit> found;
     uint32_t nfound = 0;
@@ -803,6 +891,11 @@ void serve_loop(hss_t* h) {
         {
             std::lock_guard<std::mutex> g(h->gpu_mu);
             s = begin_call(h, rows.size());
+            if (!s) {
+                std::vector<uint64_t> ls(rows.size());
+                for (size_t i = 0; i < rows.size(); ++i) ls[i] = rows[i].l;
+                s = upload_row_info(h, ls);
+            }
             if (!s) s = run_batched(h, rows);
             if (!s) s = end_call(h, rows.size(), &ms, &found, &nfound);
         }

@@ -14,22 +14,28 @@
 // How it is computed here.  The reference multiplies every product out in
 // 128-bit arithmetic.  These kernels decide almost every product from
 //   * residues of the product's coordinates mod 720, 625 and 1547, formed from
-//     per-value residues (exact, 32-bit integer multiplies), and
-//   * float approximations of the coordinates with a proven error bound
-//     (|z| = 2 l^2 m^2 is known per pair, so every coordinate error is below
-//     eps = 2 l^2 m^2 * 2^-20),
-// and send a product to the exact 128-bit path only when a window decision is
-// within eps of a boundary, or when its z survives every residue filter (a
-// possible hit).  Candidate counts are therefore exact, and every hit is
-// confirmed exactly and rechecked in 256-bit arithmetic.
+//     per-value residues with 32-bit multiplies (exact), and
+//   * float coordinates with a proven error bound: |z| = 2 l^2 m^2 is known per
+//     pair, so every coordinate's float error is below eps = 2 l^2 m^2 2^-20,
+// and only go to exact 128-bit arithmetic when a decision is within eps of a
+// window boundary, or when z passes every residue filter and a fourth root n
+// inside z's float bounds matches z modulo 720 * 625 * 1547 (a possible hit).
+// Counts are therefore exact and every hit is confirmed exactly and rechecked
+// in 256-bit arithmetic.
+//
+// The hot loop is branch-free per (alpha, beta) value pair.  Work that only
+// a few lanes need (deep residue filters, the fourth-root filter, undecided
+// products, products whose both orientations pass the area test) is written
+// to a per-warp queue of events and processed 32 at a time with every lane
+// busy, outside the hot loop.
 //
 // Work shapes.  batched_kernel is persistent: CTAs pull (row l, m-range)
-// items from a global cursor; the m-side values of the range are read once,
-// coalesced, and each thread multiplies its value against the row's whole
-// segment held in shared memory (a uniform loop: no per-pair divergence).
-// plain_kernel keeps the reference's shape (a block per (row, slice), one
-// thread per pair).  merged_kernel handles the pairs that share a split prime
-// (gpu_search_v42.cu:318-341), one CTA per pair.
+// items from a global cursor; per item the valid m-side records are compacted
+// into shared memory and processed in lockstep rounds against the row's
+// segment, also in shared memory.  plain_kernel keeps the reference's shape
+// (a block per (row, slice), one thread per pair).  merged_kernel (a warp per
+// pair) and merged_big_kernel (a CTA per pair) handle the pairs that share a
+// split prime (gpu_search_v42.cu:318-341).
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -45,40 +51,45 @@ constexpr uint32_t kSqA = kModA * kModA;
 constexpr uint32_t kSqB = kModB * kModB;
 constexpr uint32_t kSqC = kModC * kModC;
 constexpr uint32_t kTabA = 0, kTabB = 720, kTabC = 720 + 625;
-constexpr uint32_t kSlices = 8;           // plain kernel: blocks per row
-constexpr uint32_t kPlainThreads = 128;   // plain kernel: threads per block
+constexpr uint32_t kSlices = 8;            // plain kernel: blocks per row
+constexpr uint32_t kPlainThreads = 128;    // plain kernel: threads per block
 constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
-constexpr uint32_t kMergedListCap = 2048;  // alpha + beta entries of one big pair
+constexpr uint32_t kMergedListCap = 1536;  // alpha + beta entries of one big pair
 constexpr uint32_t kWarpPairThreads = 256; // shared-prime pairs: one warp per pair
 constexpr uint32_t kWarpPairWarps = kWarpPairThreads / 32;
-constexpr uint32_t kWarpListCap = 192;     // alpha + beta entries of one warp's pair
+constexpr uint32_t kWarpListCap = 160;     // alpha + beta entries of one warp's pair
 constexpr uint32_t kMaxTerms = 16;
+constexpr uint32_t kQueue = 64;            // events per warp queue
+constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 // Window and filter constants of one pair (l, m).
 struct PairCtx {
-    float lo1, hi1, lo1o, hi1o;  // z = S - t counted iff t in [lo1, hi1]; not iff t < lo1o or t > hi1o
-    float hi2, hi2o;             // z = S + t counted iff t <= hi2; not iff t > hi2o
+    float lo1, hi1, lo1o, hi1o;  // z = S - t counted iff t in [lo1, hi1]; maybe iff t in [lo1o, hi1o]
+    float hi2, hi2o;             // z = S + t counted iff t <= hi2; maybe iff t <= hi2o
     float eps;                   // bound on |float - exact| of a product coordinate
-    uint32_t sres;               // S = l^4 + m^4 mod 720 | mod 625 << 10 | mod 1547 << 20 | flag5 << 31
+    float sf;                    // S = l^4 + m^4 as float
+    uint32_t sres;               // S mod 720 | mod 625 << 10 | mod 1547 << 20 | flag5 << 31
     uint32_t dinv;               // inverse of D mod 2^32 (0: pair not on this path)
     uint32_t dthr;               // floor((2^32 - 1) / (8 D))
+    uint32_t m;
 };
 
-// Constants of one root row.
-struct RowConst {
-    uint64_t l, l2;
-    u128 l4, n4;
-    uint32_t lmodA, lmodB, lmodC;   // l^4 mod 720, 625, 1547
-    uint32_t l2modA;                // l^2 mod 720
-    uint32_t l3, l5, leven;
-    uint32_t nprimes;               // odd primes of l
-    uint32_t pinv[9], pthr[9], psplit[9];
-    uint32_t free_l;                // |free(l)|
+// Row-side value in shared memory: coordinates as float and their mod-720
+// residues (bit 31 of ra: central value); B/C residues kept alongside.
+struct AlphaHot {
+    float re, im;
+    uint32_t ra, ia;
 };
 
 struct Acc {
     uint32_t cand, r16, prod, exact, processed, merged;
 };
+
+// Event flags per product p (bits 4p .. 4p+3).
+constexpr uint32_t kEvU = 1;   // undecided: count the whole product exactly
+constexpr uint32_t kEvDx = 2;  // orientation (x, y) counted, z passed mod 720: deep + root filters
+constexpr uint32_t kEvDy = 4;  // the same for orientation (y, x)
+constexpr uint32_t kEvB = 8;   // non-dual pair with both orientations gated: (y, x) still to do
 
 // ------------------------------------------------------------ arithmetic
 
@@ -107,20 +118,25 @@ __host__ __device__ inline uint32_t inverse_odd(uint32_t d) {
     return x;
 }
 
-__device__ inline bool divides(uint32_t inv, uint32_t thr, uint32_t m) { return m * inv <= thr; }
+__device__ __forceinline__ bool divides(uint32_t inv, uint32_t thr, uint32_t m) { return m * inv <= thr; }
 
-// n = 0 mod 8D for n < 2^29, via one multiply and a rotate: n * D^-1 mod 2^32
-// rotated right by 3 is at most floor((2^32-1)/(8D)) exactly when 8D | n.
+// 8D | n via one multiply and a rotate: n * D^-1 mod 2^32 rotated right by 3
+// is at most floor((2^32-1)/(8D)) exactly when 8D divides n.
 __device__ __forceinline__ bool area_gate(uint32_t n, uint32_t dinv, uint32_t dthr) {
     uint32_t h = n * dinv;
     return __funnelshift_r(h, h, 3) <= dthr;
 }
 
+__host__ __device__ __forceinline__ uint32_t pow4_mod(uint32_t x, uint32_t m) {
+    uint32_t s = x * x % m;
+    return s * s % m;
+}
+
 // ----------------------------------------------------------- 256-bit check
 
-// Heron recheck (the reference's CPU does it on the host, search_v18.cpp:
-// 481-501): the four Heron factors of sides l^2, m^2, n^2 are positive and
-// their product equals (4A)^2, compared in 256-bit arithmetic.
+// Heron recheck (done on the host by the reference's CPU search,
+// search_v18.cpp:481-501): the four Heron factors of sides l^2, m^2, n^2 are
+// positive and their product equals (4A)^2, compared in 256-bit arithmetic.
 __device__ void mul256(const uint64_t a[4], const uint64_t b[4], uint64_t out[4]) {
     uint64_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int i = 0; i < 4; ++i) {
@@ -184,18 +200,17 @@ __device__ ExactPair exact_pair(uint64_t l, uint64_t m, uint64_t n, uint32_t row
 }
 
 // The candidate test of one signed D (gpu_search_v42.cu:158-179): counted on
-// entry; then z = l^4 + m^4 - D is tested exactly.
+// entry; then z = l^4 + m^4 - D is tested exactly.  The residue tables hold
+// necessary conditions for z = n^4 (with 5 | n when 5 divides neither l nor
+// m); the fourth root itself is found and checked in 128-bit arithmetic.
 __device__ void exact_test_d(const ExactPair& p, i128 d, i128 area4, uint32_t& cand, uint32_t& r16,
                              const uint8_t* tab, const LaunchBuffers& buf) {
     ++cand;
     i128 sz = (i128)p.l4 + (i128)p.m4 - d;
     if (sz < 0 || (u128)sz < p.m4 || (u128)sz > p.n4) return;
     u128 z = (u128)sz;
-    uint32_t low = (uint32_t)z & 15u;
-    if (low > 1) return;
+    if (((uint32_t)z & 15u) > 1u) return;
     ++r16;
-    // necessary conditions for z = n^4 (with 5 | n when 5 divides neither l
-    // nor m): z mod 720 (16, 9, 5), mod 625 and mod 7*13*17, from the tables
     uint32_t rA = mod_u128_small(z, kModA), rB = mod_u128_small(z, kModB);
     if (!(tab[kTabA + rA] & ((p.flags & 2u) ? 4u : 2u))) return;
     if ((p.flags & 2u) ? rB != 0 : !tab[kTabB + rB]) return;
@@ -236,179 +251,276 @@ __device__ void exact_test_pair(const ExactPair& p, i128 d, i128 area4, uint32_t
     if (neg && d != 0) exact_test_d(p, -d, area4, cand, r16, tab, buf);
 }
 
-// Both orientations of the product x + iy (gpu_search_v42.cu:196-200).
-__device__ void exact_product(const ExactPair& p, i128 x, i128 y, uint32_t& cand, uint32_t& r16,
-                              const uint8_t* tab, const LaunchBuffers& buf) {
-    exact_test_pair(p, x, y, cand, r16, tab, buf);
-    if (x != y && x != -y) exact_test_pair(p, y, x, cand, r16, tab, buf);
-}
-
-// Resolves the products flagged by eval_pair: status bit k (k = 0: a*b,
-// k = 1: a*conj(b)) means "undecided: count exactly", bit 2+k means "possible
-// hit: test exactly, counts already taken".
-__device__ __noinline__ void resolve_exact(uint32_t st, i128 ar, i128 ai, i128 br, i128 bi, uint64_t l, uint64_t m,
-                              uint64_t n, uint32_t row, const uint8_t* tab, Acc& acc, const LaunchBuffers& buf) {
+// Exact evaluation of the product (ar + i ai) * (br + i bi), or of
+// (ar + i ai) * conj(br + i bi) when conj_b, for the orientations in `omask`
+// (bit 0: (D, 4A) = (x, y); bit 1: (y, x), taken only when x != +-y as in
+// gpu_search_v42.cu:196-200).  Hits are recorded; counts are returned.
+__device__ __noinline__ void exact_eval(i128 ar, i128 ai, i128 br, i128 bi, bool conj_b, uint32_t omask,
+                                        uint64_t l, uint64_t m, uint64_t n, uint32_t row, const uint8_t* tab,
+                                        const LaunchBuffers& buf, uint32_t* cand, uint32_t* r16) {
     ExactPair p = exact_pair(l, m, n, row);
-    for (int k = 0; k < 2; ++k) {
-        if (!(st & ((1u | 4u) << k))) continue;
-        i128 bim = k ? -bi : bi;
-        i128 x = ar * br - ai * bim, y = ar * bim + ai * br;
-        uint32_t c = 0, r = 0;
-        exact_product(p, x, y, c, r, tab, buf);
-        if (st & (1u << k)) {
-            acc.cand += c;
-            acc.r16 += r;
-            acc.exact += 1;
-        }
-    }
+    i128 bim = conj_b ? -bi : bi;
+    i128 x = ar * br - ai * bim, y = ar * bim + ai * br;
+    uint32_t c = 0, r = 0;
+    if (omask & 1u) exact_test_pair(p, x, y, c, r, tab, buf);
+    if ((omask & 2u) && x != y && x != -y) exact_test_pair(p, y, x, c, r, tab, buf);
+    *cand = c;
+    *r16 = r;
 }
 
-// --------------------------------------------------------------- fast path
+// ------------------------------------------------------------ fast path
 
-// Deeper residue filters mod 625 and 1547 for a counted orientation whose z
-// passed the mod-720 table; true when some counted sign survives.
-__device__ __forceinline__ bool deep_filters(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw,
-                                             int k, int o, bool neg, bool c1, bool c2, uint32_t sres,
-                                             bool flag5, const uint8_t* tab) {
-    uint32_t ar = (arw >> 10) & 1023u, ai = (aiw >> 10) & 1023u, br = (brw >> 10) & 1023u,
-             bi = (biw >> 10) & 1023u;
-    uint32_t q1 = ar * br, q2 = ai * bi, q3 = ar * bi, q4 = ai * br;
-    uint32_t x = k ? q1 + q2 : q1 + kSqB - q2;
-    uint32_t y = k ? q4 + kSqB - q3 : q3 + q4;
-    uint32_t dB = (o ? y : x) % kModB;
-    uint32_t tB = neg ? (dB ? kModB - dB : 0u) : dB;
-    uint32_t sB = (sres >> 10) & 1023u;
-    uint32_t zB1 = sB >= tB ? sB - tB : sB + kModB - tB;
-    uint32_t zB2 = sB + tB >= kModB ? sB + tB - kModB : sB + tB;
-    bool okB1 = flag5 ? zB1 == 0 : tab[kTabB + zB1] != 0;
-    bool okB2 = flag5 ? zB2 == 0 : tab[kTabB + zB2] != 0;
-    c1 = c1 && okB1;
-    c2 = c2 && okB2;
-    if (!(c1 || c2)) return false;
-    ar = (arw >> 20) & 2047u;
-    ai = (aiw >> 20) & 2047u;
-    br = (brw >> 20) & 2047u;
-    bi = (biw >> 20) & 2047u;
-    q1 = ar * br;
-    q2 = ai * bi;
-    q3 = ar * bi;
-    q4 = ai * br;
-    x = k ? q1 + q2 : q1 + kSqC - q2;
-    y = k ? q4 + kSqC - q3 : q3 + q4;
-    uint32_t dC = (o ? y : x) % kModC;
-    uint32_t tC = neg ? (dC ? kModC - dC : 0u) : dC;
-    uint32_t sC = (sres >> 20) & 2047u;
-    uint32_t zC1 = sC >= tC ? sC - tC : sC + kModC - tC;
-    uint32_t zC2 = sC + tC >= kModC ? sC + tC - kModC : sC + tC;
-    return (c1 && tab[kTabC + zC1]) || (c2 && tab[kTabC + zC2]);
+struct Window {
+    bool in1, in2, und;
+};
+
+// Window decision for t = |D| from its float value: counted terms (z = S - t
+// and z = S + t) and whether any boundary is within the error bound.
+__device__ __forceinline__ Window window(float t, const PairCtx& c) {
+    Window w;
+    w.in1 = (t >= c.lo1) & (t <= c.hi1);
+    w.in2 = t <= c.hi2;
+    bool maybe1 = (t >= c.lo1o) & (t <= c.hi1o);
+    bool maybe2 = t <= c.hi2o;
+    // a counted term also needs the sign of D, certain once t > eps
+    w.und = (maybe1 & !w.in1) | (maybe2 & !w.in2) | ((w.in1 | w.in2) & (t < c.eps));
+    return w;
 }
 
-// One product x + iy (float xf, yf; mod-720 residues xa, ya as unreduced
-// sums).  Adds its candidates to acc when every decision is certain and
-// returns 0, 1 (undecided) or 4 (possible hit), shifted by k by the caller.
-__device__ __forceinline__ uint32_t eval_product(float xf, float yf, uint32_t xa, uint32_t ya, int k,
-                                                 uint32_t arw, uint32_t aiw, uint32_t brw,
-                                                 uint32_t biw, const PairCtx& c, const uint8_t* tab,
-                                                 Acc& acc) {
-    uint32_t cnt = 0, r = 0, status = 0;
-    const bool flag5 = (c.sres >> 31) != 0;
+__device__ __forceinline__ uint32_t add_mod(uint32_t a, uint32_t b, uint32_t m) {
+    uint32_t s = a + b;
+    return s >= m ? s - m : s;
+}
+
+__device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t m) {
+    return a >= b ? a - b : a + m - b;
+}
+
+// Hot evaluation of one (alpha, beta) value pair: products p = 0 (alpha*beta)
+// and, when neither value is central, p = 1 (alpha*conj(beta)).  Counts the
+// candidates and mod-16 survivors it can decide; returns event flags for the
+// rest (0 for nearly all pairs).
+//
+// Which orientations can pass the area test is a property of the pair: when
+// l*m is even and 3 and 5 both divide l*m, both coordinates of every product
+// are = 0 mod 8*9 (the powers of 1+i and of 3 in 2 l^2 m^2 divide both) and
+// no mod-5 condition applies, so both orientations pass (DUAL).  Otherwise at
+// most one does: for odd l*m only the coordinate with the higher power of 2 is
+// = 0 mod 8; if 3 (or 5) does not divide 2 l^2 m^2 it divides at most one leg
+// of the triple (x, y, 2 l^2 m^2).  The non-dual path evaluates the one gated
+// orientation and raises kEvB if both ever pass, so it stays exact regardless.
+template <bool DUAL>
+__device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t bra, uint32_t bia,
+                                              bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc) {
+    const bool ca = (a.ra >> 31) != 0;
+    const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
+    const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
+    const float f1 = a.re * br, f2 = a.im * bi, f3 = a.re * bi, f4 = a.im * br;
     const uint32_t sA = c.sres & 1023u;
+    const uint32_t sel = (c.sres >> 31) ? 4u : 2u;
+    uint32_t flags = 0, cnt = 0, r16 = 0;
 #pragma unroll
-    for (int o = 0; o < 2; ++o) {
-        uint32_t ares = o ? xa : ya;
-        if (!area_gate(ares, c.dinv, c.dthr)) continue;
-        float df = o ? yf : xf;
-        float t = fabsf(df);
-        bool in1 = (t >= c.lo1) & (t <= c.hi1);
-        bool in2 = t <= c.hi2;
-        bool und = (!in1 & (t >= c.lo1o) & (t <= c.hi1o)) | (!in2 & (t <= c.hi2o)) | (t < c.eps);
-        if (und) {
-            status |= 1u;
+    for (int p = 0; p < 2; ++p) {
+        const bool valid = p == 0 ? !(ca & cb) : !(ca | cb);
+        const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
+        const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
+        const float xf = p ? f1 + f2 : f1 - f2;
+        const float yf = p ? f4 - f3 : f3 + f4;
+        const bool gx = valid & area_gate(Y, c.dinv, c.dthr);  // (D, 4A) = (x, y)
+        const bool gy = valid & area_gate(X, c.dinv, c.dthr);  // (D, 4A) = (y, x)
+        uint32_t f = 0, pc = 0, pr = 0;
+        bool und = false;
+#pragma unroll
+        for (int o = 0; o < (DUAL ? 2 : 1); ++o) {
+            // DUAL: o = 0 is (x, y), o = 1 is (y, x); otherwise the gated one
+            const bool g = DUAL ? (o ? gy : gx) : (gx | gy);
+            const bool oy = DUAL ? (o == 1) : !gx;
+            const float d = oy ? yf : xf;
+            const uint32_t dres = oy ? Y : X;
+            const Window w = window(fabsf(d), c);
+            und |= g & w.und;
+            const bool ok = g & !w.und;
+            const uint32_t dA = dres % kModA;
+            const uint32_t tA = d < 0.f ? (dA ? kModA - dA : 0u) : dA;
+            const uint32_t z1 = sub_mod(sA, tA, kModA), z2 = add_mod(sA, tA, kModA);
+            const uint32_t m1 = (ok & w.in1) ? tab[kTabA + z1] : 0u;
+            const uint32_t m2 = (ok & w.in2) ? tab[kTabA + z2] : 0u;
+            pc += ok ? (uint32_t)w.in1 + (uint32_t)w.in2 : 0u;
+            pr += (m1 & 1u) + (m2 & 1u);
+            f |= ((m1 | m2) & sel) ? (oy ? kEvDy : kEvDx) : 0u;
+        }
+        if (!DUAL) f |= (gx & gy) ? kEvB : 0u;
+        // an undecided product is counted whole on the exact path instead
+        cnt += und ? 0u : pc;
+        r16 += und ? 0u : pr;
+        flags |= (und ? kEvU : f) << (4 * p);
+    }
+    acc.cand += cnt;
+    acc.r16 += r16;
+    acc.prod += (ca | cb) ? ((ca & cb) ? 0u : 1u) : 2u;
+    return flags;
+}
+
+// A possible hit needs some n in [m, N] with n^4 = z.  From z's float bounds
+// (|error| below sf 2^-22 + eps + |z| 2^-22) take the n with n^4 inside them
+// (plus a margin for the float fourth root: n < 2^25, so a relative 2^-20
+// and 2 units cover it) and keep the candidate only if some such n has
+// n^4 = z mod 720, 625 and 1547.  Float and 32-bit integer arithmetic only.
+__device__ bool root_filter(float zf, const PairCtx& c, uint32_t zA, uint32_t zB, uint32_t zC, uint32_t n_limit) {
+    const float ez = c.sf * 0x1p-22f + c.eps + fabsf(zf) * 0x1p-22f;
+    const float lo = fmaxf(zf - ez, 0.f), hi = zf + ez;
+    const float rlo = sqrtf(sqrtf(lo)) * (1.f - 0x1p-20f), rhi = sqrtf(sqrtf(hi)) * (1.f + 0x1p-20f);
+    const uint32_t m = c.m & 0x7FFFFFFFu;
+    const uint32_t flo = __float2uint_rd(rlo), fhi = __float2uint_ru(rhi);
+    const uint32_t nlo = flo > m + 2 ? flo - 2 : m;
+    const uint32_t nhi = fhi + 2 < n_limit ? fhi + 2 : n_limit;
+    for (uint32_t n = nlo; n <= nhi; ++n) {
+        if (pow4_mod(n % kModA, kModA) != zA) continue;
+        if (pow4_mod(n % kModB, kModB) != zB) continue;
+        if (pow4_mod(n % kModC, kModC) != zC) continue;
+        return true;
+    }
+    return false;
+}
+
+// Residues of the product's coordinates modulo 625 (field 1) or 1547
+// (field 2) from the packed value residues.
+__device__ __forceinline__ void coord_res(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw, int field,
+                                          int p, uint32_t& x, uint32_t& y) {
+    const uint32_t shift = field == 1 ? 10u : 20u;
+    const uint32_t mask = field == 1 ? 1023u : 2047u;
+    const uint32_t M = field == 1 ? kModB : kModC;
+    const uint32_t sq = field == 1 ? kSqB : kSqC;
+    uint32_t ar = (arw >> shift) & mask, ai = (aiw >> shift) & mask, br = (brw >> shift) & mask,
+             bi = (biw >> shift) & mask;
+    uint32_t q1 = ar * br, q2 = ai * bi, q3 = ar * bi, q4 = ai * br;
+    x = (p ? q1 + q2 : q1 + sq - q2) % M;
+    y = (p ? q4 + sq - q3 : q3 + q4) % M;
+}
+
+// Exact coordinates for the rare exact path.
+struct ExactValues {
+    __int128 ar, ai, br, bi;
+};
+
+__device__ __forceinline__ uint32_t pair_m(const PairCtx& c) { return c.m & 0x7FFFFFFFu; }
+__device__ __forceinline__ bool pair_dual(const PairCtx& c) { return (c.m >> 31) != 0; }
+
+// Exact work raised by an event, done later by exact_kernel: count a whole
+// product, count one orientation, or test one orientation for a hit.
+constexpr uint32_t kExCount = 0, kExOrient = 1, kExHit = 2;
+
+// Work of one event (one lane), in float and 32-bit integer arithmetic only:
+// an undecided product is queued for exact counting; the (y, x) orientation
+// of a non-dual product whose both orientations passed is decided and
+// counted; every counted orientation whose z passed mod 720 goes through the
+// mod-625 / mod-1547 filters and the fourth-root filter, and survivors are
+// queued for the exact hit test.  push(kind | p << 2 | o << 3) queues work.
+template <class PushFn>
+__device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a, uint32_t arw, uint32_t aiw,
+                                              const HotRec& b, const PairCtx& c, uint32_t n_limit,
+                                              const uint8_t* tab, Acc& acc, PushFn push) {
+    const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
+    const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+    const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
+    const float f1 = a.re * b.re, f2 = a.im * b.im, f3 = a.re * b.im, f4 = a.im * b.re;
+    const uint32_t sA = c.sres & 1023u, sB = (c.sres >> 10) & 1023u, sC = (c.sres >> 20) & 2047u;
+    const bool flag5 = (c.sres >> 31) != 0;
+    const uint32_t sel = flag5 ? 4u : 2u;
+    for (int p = 0; p < 2; ++p) {
+        const uint32_t f = (flags >> (4 * p)) & 15u;
+        if (!f) continue;
+        if (f & kEvU) {
+            push(kExCount | (uint32_t)p << 2);
             continue;
         }
-        if (!(in1 | in2)) continue;
-        cnt += (uint32_t)in1 + (uint32_t)in2;
-        bool neg = df < 0.f;
-        uint32_t dA = (o ? ya : xa) % kModA;
-        uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
-        uint32_t z1 = sA >= tA ? sA - tA : sA + kModA - tA;
-        uint32_t z2 = sA + tA >= kModA ? sA + tA - kModA : sA + tA;
-        uint32_t m1 = in1 ? tab[kTabA + z1] : 0u;
-        uint32_t m2 = in2 ? tab[kTabA + z2] : 0u;
-        r += (m1 & 1u) + (m2 & 1u);
-        uint32_t sel = flag5 ? 4u : 2u;
-        if ((m1 | m2) & sel) {
-            if (deep_filters(arw, aiw, brw, biw, k, o, neg, (m1 & sel) != 0, (m2 & sel) != 0, c.sres,
-                             flag5, tab))
-                status |= 4u;
+        const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
+        const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
+        const float xf = p ? f1 + f2 : f1 - f2;
+        const float yf = p ? f4 - f3 : f3 + f4;
+        for (int o = 0; o < 2; ++o) {
+            const bool full = o == 1 && (f & kEvB);
+            const bool deep = (f & (o ? kEvDy : kEvDx)) != 0;
+            if (!full && !deep) continue;
+            const float d = o ? yf : xf;
+            const float t = fabsf(d);
+            const Window w = window(t, c);
+            if (full) {
+                if (w.und) {
+                    push(kExOrient | (uint32_t)p << 2 | (uint32_t)o << 3);
+                    continue;
+                }
+                acc.cand += (uint32_t)w.in1 + (uint32_t)w.in2;
+            }
+            const uint32_t dA = (o ? Y : X) % kModA;
+            const bool neg = d < 0.f;
+            const uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
+            const uint32_t zA1 = sub_mod(sA, tA, kModA), zA2 = add_mod(sA, tA, kModA);
+            const uint32_t m1 = w.in1 ? tab[kTabA + zA1] : 0u, m2 = w.in2 ? tab[kTabA + zA2] : 0u;
+            if (full) acc.r16 += (m1 & 1u) + (m2 & 1u);
+            if (!((m1 | m2) & sel)) continue;
+            uint32_t xB, yB, xC, yC;
+            coord_res(arw, aiw, b.rre, b.rim, 1, p, xB, yB);
+            coord_res(arw, aiw, b.rre, b.rim, 2, p, xC, yC);
+            const uint32_t dB = o ? yB : xB, dC = o ? yC : xC;
+            const uint32_t tB = neg ? (dB ? kModB - dB : 0u) : dB, tC = neg ? (dC ? kModC - dC : 0u) : dC;
+            bool hit_possible = false;
+            for (int term = 0; term < 2 && !hit_possible; ++term) {
+                const uint32_t mm = term ? m2 : m1;
+                if (!(mm & sel)) continue;
+                const uint32_t zB = term ? add_mod(sB, tB, kModB) : sub_mod(sB, tB, kModB);
+                const uint32_t zC = term ? add_mod(sC, tC, kModC) : sub_mod(sC, tC, kModC);
+                if (flag5 ? zB != 0 : !tab[kTabB + zB]) continue;
+                if (!tab[kTabC + zC]) continue;
+                const float zf = term ? c.sf + t : c.sf - t;
+                if (root_filter(zf, c, term ? zA2 : zA1, zB, zC, n_limit)) hit_possible = true;
+            }
+            if (hit_possible) push(kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
         }
     }
-    if (status & 1u) return 1u;
-    acc.cand += cnt;
-    acc.r16 += r;
-    return status;
 }
 
-// One (alpha, beta) value pair: products alpha*beta and, when neither value
-// is central, alpha*conj(beta).  Returns the exact-path status bits.
-__device__ __forceinline__ uint32_t eval_pair(const HotRec& a, const HotRec& b, bool two,
-                                              const PairCtx& c, const uint8_t* tab, Acc& acc) {
-    uint32_t ar = a.rre & 1023u, ai = a.rim & 1023u, br = b.rre & 1023u, bi = b.rim & 1023u;
-    uint32_t p1 = ar * br, p2 = ai * bi, p3 = ar * bi, p4 = ai * br;
-    float f1 = a.re * b.re, f2 = a.im * b.im, f3 = a.re * b.im, f4 = a.im * b.re;
-    uint32_t st = eval_product(f1 - f2, f3 + f4, p1 + kSqA - p2, p3 + p4, 0, a.rre, a.rim, b.rre, b.rim,
-                               c, tab, acc);
-    if (two) {
-        uint32_t s2 = eval_product(f1 + f2, f4 - f3, p1 + p2, p4 + kSqA - p3, 1, a.rre, a.rim, b.rre,
-                                   b.rim, c, tab, acc);
-        st |= s2 << 1;
-    }
-    return st;
+// Appends one exact work item (a, b: exact-value indices; for shared-prime
+// pairs, list entries) to the global exact queue.
+__device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t kind, uint32_t a, uint32_t b, uint32_t l,
+                                           uint32_t m, uint32_t row, bool shared_prime) {
+    unsigned int idx = atomicAdd(buf.exact_count, 1u);
+    if (idx < buf.exact_cap)
+        buf.exact_queue[idx] = ExactItem{kind | (shared_prime ? 16u : 0u), a, b, l, m, row, 0u, 0u};
+    else
+        atomicOr(buf.error_flags, 4u);
+}
+
+// Event handler of the cached path: record j against the row value whose
+// exact value is at index ka; counts come back by value (x: candidates, y:
+// mod-16 survivors).
+__device__ __forceinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
+                                              uint32_t j, uint32_t l, uint32_t row, const uint8_t* tab,
+                                              uint32_t limit, const LaunchBuffers* buf) {
+    Acc acc{0, 0, 0, 0, 0, 0};
+    process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
+                  [&](uint32_t kind) { push_exact(*buf, kind, ka, j, l, pair_m(c), row, false); });
+    return make_uint2(acc.cand, acc.r16);
+}
+
+__device__ __forceinline__ void add_event(Acc& acc, uint2 r) {
+    acc.cand += r.x;
+    acc.r16 += r.y;
 }
 
 // ------------------------------------------------------------ pair set-up
-
-__device__ __noinline__ void row_setup(const DeviceCache& cache, uint64_t l, RowConst& R) {
-    uint64_t n = cache.limit;
-    R.l = l;
-    R.l2 = l * l;
-    R.l4 = (u128)R.l2 * R.l2;
-    R.n4 = (u128)(n * n) * (n * n);
-    R.lmodA = mod_u128_small(R.l4, kModA);
-    R.lmodB = mod_u128_small(R.l4, kModB);
-    R.lmodC = mod_u128_small(R.l4, kModC);
-    R.l2modA = (uint32_t)(R.l2 % kModA);
-    R.l3 = l % 3 == 0;
-    R.l5 = l % 5 == 0;
-    R.leven = (l & 1) == 0;
-    R.free_l = cache.seg_off[l + 1] - cache.seg_off[l] - 1;
-    uint32_t np = 0;
-    uint64_t x = l;
-    while (x > 1) {
-        uint32_t p = cache.spf[x];
-        do x /= p;
-        while (x % p == 0);
-        if (p == 2) continue;
-        R.pinv[np] = inverse_odd(p);
-        R.pthr[np] = 0xFFFFFFFFu / p;
-        R.psplit[np] = (p & 3u) == 1u;
-        ++np;
-    }
-    R.nprimes = np;
-}
 
 enum PairKind : uint32_t { kSkip = 0, kCached = 1, kMerged = 2 };
 
 // Skip rules of gpu_search_v42.cu:305-316 (and search_v18.cpp:336-339, 362):
 // both even; an inert prime of l dividing m; neither has a split prime.
 // A split prime of l dividing m sends the pair to the shared-prime path.
-__device__ __forceinline__ uint32_t classify(const RowConst& R, const DeviceCache& cache, uint32_t m,
-                                             uint32_t free_m) {
+__device__ __forceinline__ uint32_t classify(const RowInfo& R, uint32_t m, uint32_t free_m) {
     if (R.leven && (m & 1u) == 0) return kSkip;
     bool shared_split = false;
-    for (uint32_t i = 0; i < R.nprimes; ++i) {
+    for (uint32_t i = 0; i < R.nodd; ++i) {
         if (divides(R.pinv[i], R.pthr[i], m)) {
-            if (!R.psplit[i]) return kSkip;
+            if (!((R.psplit >> i) & 1u)) return kSkip;
             shared_split = true;
         }
     }
@@ -416,16 +528,11 @@ __device__ __forceinline__ uint32_t classify(const RowConst& R, const DeviceCach
     return shared_split ? kMerged : kCached;
 }
 
-__device__ __forceinline__ uint32_t pow4_mod(uint32_t x, uint32_t m) {
-    uint32_t s = x * x % m;
-    return s * s % m;
-}
-
 // Window and filter constants for pair (l, m); also the analytic count of
 // the all-central product (2 l^2 m^2, 0), whose only orientation with a
 // nonzero area is D = 0, 4A = 2 l^2 m^2 (counted when the window contains 0;
 // z = l^4 + m^4 is never a fourth power).
-__device__ __noinline__ PairCtx make_ctx(const RowConst& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16) {
+__device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16) {
     uint64_t m2 = m * m;
     u128 m4 = (u128)m2 * m2;
     i128 w = (i128)R.l4 + (i128)m4 - (i128)R.n4;
@@ -444,14 +551,19 @@ __device__ __noinline__ PairCtx make_ctx(const RowConst& R, uint64_t m, uint32_t
         c.hi2 = -INFINITY;
         c.hi2o = -INFINITY;
     } else {
-        c.lo1 = -1.f;   // non-central products have |D| >= 1 > 0 = max(w, 0)
+        c.lo1 = -1.f;  // non-central products have |D| >= 1 > 0 = max(w, 0)
         c.lo1o = -2.f;
         c.hi2 = -wf - ew;
         c.hi2o = -wf + ew;
     }
     c.eps = E;
+    c.sf = u128_to_float(R.l4 + m4);
     bool f3 = R.l3 || m % 3 == 0;
     bool f5 = !R.l5 && m % 5 != 0;
+    // both orientations pass the area test for every product exactly when
+    // l*m is even and 3 and 5 both divide l*m (see eval_fast)
+    const bool dual = (R.leven || (m & 1) == 0) && f3 && !f5;
+    c.m = (uint32_t)m | (dual ? 0x80000000u : 0u);
     uint32_t D = 3u * (f3 ? 3u : 1u) * (f5 ? 5u : 1u);
     c.dinv = inverse_odd(D);
     c.dthr = 0xFFFFFFFFu / (8u * D);
@@ -460,7 +572,6 @@ __device__ __noinline__ PairCtx make_ctx(const RowConst& R, uint64_t m, uint32_t
     uint32_t sB = (R.lmodB + pow4_mod(mB, kModB)) % kModB;
     uint32_t sC = (R.lmodC + pow4_mod(mC, kModC)) % kModC;
     c.sres = sA | (sB << 10) | (sC << 20) | (f5 ? 0x80000000u : 0u);
-    // all-central product: 4A = 2 l^2 m^2 must be = 0 mod 8D and w <= 0
     uint32_t areaA = 2u * (R.l2modA * (uint32_t)(m2 % kModA) % kModA);
     bool cc = area_gate(areaA, c.dinv, c.dthr) && w <= 0;
     cc_cand = cc ? 1u : 0u;
@@ -468,23 +579,24 @@ __device__ __noinline__ PairCtx make_ctx(const RowConst& R, uint64_t m, uint32_t
     return c;
 }
 
-__device__ __forceinline__ HotRec scale2(HotRec h) {
-    HotRec s;
-    s.re = 2.f * h.re;
-    s.im = 2.f * h.im;
-    uint32_t ra = h.rre & 1023u, rb = (h.rre >> 10) & 1023u, rc = (h.rre >> 20) & 2047u;
-    ra = 2 * ra >= kModA ? 2 * ra - kModA : 2 * ra;
-    rb = 2 * rb >= kModB ? 2 * rb - kModB : 2 * rb;
-    rc = 2 * rc >= kModC ? 2 * rc - kModC : 2 * rc;
-    s.rre = ra | (rb << 10) | (rc << 20) | (h.rre & kCentralBit);
-    ra = h.rim & 1023u;
-    rb = (h.rim >> 10) & 1023u;
-    rc = (h.rim >> 20) & 2047u;
-    ra = 2 * ra >= kModA ? 2 * ra - kModA : 2 * ra;
-    rb = 2 * rb >= kModB ? 2 * rb - kModB : 2 * rb;
-    rc = 2 * rc >= kModC ? 2 * rc - kModC : 2 * rc;
-    s.rim = ra | (rb << 10) | (rc << 20);
-    return s;
+// Row value alpha scaled by 2 (the factor 2 of 2 l^2 m^2; the reference
+// doubles the product instead, gpu_search_v42.cu:223-225).
+__device__ __forceinline__ void scale2(const HotRec& h, AlphaHot& a, uint2& abc) {
+    a.re = 2.f * h.re;
+    a.im = 2.f * h.im;
+    uint32_t w[2] = {h.rre, h.rim};
+    uint32_t out[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        uint32_t ra = w[i] & 1023u, rb = (w[i] >> 10) & 1023u, rc = (w[i] >> 20) & 2047u;
+        ra = 2 * ra >= kModA ? 2 * ra - kModA : 2 * ra;
+        rb = 2 * rb >= kModB ? 2 * rb - kModB : 2 * rb;
+        rc = 2 * rc >= kModC ? 2 * rc - kModC : 2 * rc;
+        out[i] = ra | (rb << 10) | (rc << 20);
+    }
+    a.ra = (out[0] & 1023u) | (h.rre & kCentralBit);
+    a.ia = out[1] & 1023u;
+    abc = make_uint2(out[0], out[1]);
 }
 
 __device__ __forceinline__ void push_merged(const LaunchBuffers& buf, uint32_t l, uint32_t m, uint32_t row) {
@@ -500,7 +612,7 @@ __device__ __forceinline__ void push_merged(const LaunchBuffers& buf, uint32_t l
 __device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc, bool shared_prime = false) {
     uint32_t v[6] = {acc.cand, acc.r16, acc.prod, acc.exact, acc.processed, acc.merged};
 #pragma unroll
-    for (int i = 0; i < 6; ++i) v[i] = __reduce_add_sync(0xFFFFFFFFu, v[i]);
+    for (int i = 0; i < 6; ++i) v[i] = __reduce_add_sync(kFull, v[i]);
     if ((threadIdx.x & 31) == 0) {
         if (v[0]) atomicAdd(&rc->candidates, (unsigned long long)v[0]);
         if (v[1]) atomicAdd(&rc->r16, (unsigned long long)v[1]);
@@ -517,107 +629,169 @@ __device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc, bool shared_p
     acc = Acc{0, 0, 0, 0, 0, 0};
 }
 
-// Products of one m-side record against the row's segment in shared memory.
-__device__ __forceinline__ void record_loop(const HotRec* s_alpha, uint32_t na, const HotRec& b,
-                                            const PairCtx& c, const uint8_t* tab, const DeviceCache& cache,
-                                            uint32_t a0, uint32_t j, uint64_t l, uint64_t m, uint32_t row,
-                                            Acc& acc, const LaunchBuffers& buf) {
-    const bool cb = (b.rre & kCentralBit) != 0;
-    for (uint32_t k = 0; k < na; ++k) {
-        HotRec a = s_alpha[k];
-        const bool ca = (a.rre & kCentralBit) != 0;
-        if (ca & cb) continue;
-        const bool two = !(ca | cb);
-        acc.prod += two ? 2u : 1u;
-        uint32_t st = eval_pair(a, b, two, c, tab, acc);
-        if (st) {
-            ExactRec ea = cache.exact[a0 + k], eb = cache.exact[j];
-            resolve_exact(st, 2 * (i128)ea.re, 2 * (i128)ea.im, (i128)eb.re, (i128)eb.im, l, m, cache.limit,
-                          row, tab, acc, buf);
-        }
-    }
+__device__ __forceinline__ uint64_t make_event(uint32_t v, uint32_t k, uint32_t flags) {
+    return (uint64_t)v | ((uint64_t)k << 16) | ((uint64_t)flags << 40);
+}
+
+// Appends the lanes' events to the warp's queue (ballot-aggregated); returns
+// true when the queue holds at least 32 events.  All 32 lanes must call it.
+__device__ __forceinline__ bool queue_push(uint64_t* q, uint32_t& count, bool has, uint64_t ev) {
+    const uint32_t mask = __ballot_sync(kFull, has);
+    if (!mask) return false;
+    const uint32_t lane = threadIdx.x & 31;
+    if (has) q[count + __popc(mask & ((1u << lane) - 1u))] = ev;
+    count += __popc(mask);
+    return count >= 32;
+}
+
+// Processes the first `n` events of a warp queue, one per lane, then moves
+// the rest to the front.  All 32 lanes must call it.
+template <class Handler>
+__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, Handler handle) {
+    __syncwarp();
+    const uint32_t lane = threadIdx.x & 31;
+    if (lane < n) handle(q[lane]);
+    __syncwarp();
+    const uint32_t rest = count - n;
+    if (lane < rest) q[lane] = q[n + lane];
+    __syncwarp();
+    count = rest;
 }
 
 // ------------------------------------------------------------ batched kernel
 
-template <int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) batched_kernel(const DeviceCache cache, const WorkItem* __restrict__ items,
-                                                     uint32_t n_items, uint32_t alpha_cap, uint32_t tile_cap,
-                                                     const LaunchBuffers buf) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    HotRec* s_alpha = reinterpret_cast<HotRec*>(smem);
-    PairCtx* s_ctx = reinterpret_cast<PairCtx*>(s_alpha + alpha_cap);
-    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_ctx + tile_cap);
-    __shared__ RowConst s_row;
-    __shared__ uint32_t s_item;
+// Persistent batched kernel.  CTAs pull items (row l, m-range); the row's
+// segment (scaled by 2) is staged in shared memory once per item.  Warps then
+// work on their own: each claims 32 roots m at a time, classifies them (one
+// per lane), keeps the pair constants in its shared slice, and walks the
+// valid m-side records in rounds of 32 - lane i of round r takes record
+// 32r + i of the concatenated segments, found with a shuffle search over the
+// lanes' prefix sums - running the row's values in lockstep.  Pairs of the
+// dual kind (both orientations live) go in a second pass of their own.
+// Events are drained from the warp queue before the warp's next 32 roots.
+struct BatchedShared {
+    uint32_t item;
+    uint32_t next_m;
+};
 
-    for (uint32_t i = threadIdx.x; i < kTableBytes; i += NT) s_tab[i] = buf.tables[i];
+__device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t owner, uint32_t k, uint32_t flags) {
+    return (uint64_t)j | ((uint64_t)owner << 32) | ((uint64_t)k << 37) | ((uint64_t)flags << 50);
+}
+
+template <bool DUAL>
+__device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint2* s_abc, uint32_t na,
+                                             const PairCtx* wctx, uint32_t cnt, uint32_t s0, uint32_t lane,
+                                             const DeviceCache& cache, const uint8_t* s_tab, uint32_t a0, uint64_t l,
+                                             uint32_t row, const LaunchBuffers& buf, uint64_t* q, uint32_t& qn,
+                                             Acc& acc) {
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= (uint32_t)d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    const uint32_t excl = incl - cnt;
+    auto handle = [&](uint64_t ev) {
+        const uint32_t j = (uint32_t)ev, owner = (uint32_t)(ev >> 32) & 31u, k = (uint32_t)(ev >> 37) & 0x1FFFu;
+        add_event(acc, cached_event((uint32_t)(ev >> 50), s_alpha[k], s_abc[k], cache.hot[j], wctx[owner], a0 + k, j,
+                                    (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf));
+    };
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t r = base + lane;
+        // owner = first lane whose inclusive prefix exceeds r
+        uint32_t owner = 0;
+#pragma unroll
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+            const uint32_t v = __shfl_sync(kFull, incl, owner + step - 1);
+            if (v <= r) owner += step;
+        }
+        owner &= 31u;
+        const uint32_t j = __shfl_sync(kFull, s0, owner) + r - __shfl_sync(kFull, excl, owner);
+        const bool live = r < total;
+        const PairCtx c = wctx[owner];
+        const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
+        const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+        const bool cb = (b.rre & kCentralBit) != 0;
+        for (uint32_t k = 0; k < na; ++k) {
+            const AlphaHot a = s_alpha[k];
+            uint32_t flags = 0;
+            if (live) flags = eval_fast<DUAL>(a, b.re, b.im, bra, bia, cb, c, s_tab, acc);
+            if (queue_push(q, qn, flags != 0, batched_event_word(j, owner, k, flags))) drain(q, qn, 32, handle);
+        }
+    }
+    while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
+}
+
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cache, const WorkItem* __restrict__ items,
+                                                           uint32_t n_items, uint32_t alpha_cap,
+                                                           const LaunchBuffers buf) {
+    constexpr uint32_t kWarps = NT / 32;
+    extern __shared__ __align__(16) unsigned char smem[];
+    AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
+    uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
+    PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_abc + alpha_cap);
+    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * 32);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_queue + kWarps * kQueue);
+    __shared__ BatchedShared S;
+
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid / 32;
+    uint64_t* q = s_queue + warp * kQueue;
+    PairCtx* wctx = s_wctx + warp * 32;
+    uint32_t qn = 0;
+    for (uint32_t i = tid; i < kTableBytes; i += NT) s_tab[i] = buf.tables[i];
     Acc acc{0, 0, 0, 0, 0, 0};
     for (;;) {
         __syncthreads();
-        if (threadIdx.x == 0) s_item = atomicAdd(buf.next_item, 1u);
-        __syncthreads();
-        const uint32_t it = s_item;
-        if (it >= n_items) break;
-        const WorkItem w = items[it];
-        if (threadIdx.x == 0) row_setup(cache, w.l, s_row);
-        __syncthreads();
-        const uint32_t a0 = cache.seg_off[w.l];
-        const uint32_t na = cache.seg_off[w.l + 1] - a0;
-        for (uint32_t i = threadIdx.x; i < na; i += NT) s_alpha[i] = scale2(cache.hot[a0 + i]);
-        const uint32_t nm = w.m1 - w.m0;
-        for (uint32_t i = threadIdx.x; i < nm; i += NT) {
-            const uint32_t m = w.m0 + i;
-            const uint32_t free_m = cache.seg_off[m + 1] - cache.seg_off[m] - 1;
-            const uint32_t kind = classify(s_row, cache, m, free_m);
-            PairCtx c;
-            c.dinv = 0;
-            if (kind == kCached) {
-                uint32_t cc_c, cc_r;
-                c = make_ctx(s_row, m, cc_c, cc_r);
-                acc.processed += 1;
-                acc.prod += 1;
-                acc.cand += cc_c;
-                acc.r16 += cc_r;
-            } else if (kind == kMerged) {
-                acc.processed += 1;
-                acc.merged += 1;
-                push_merged(buf, w.l, m, w.row);
-            }
-            s_ctx[i] = c;
+        if (tid == 0) {
+            S.item = atomicAdd(buf.next_item, 1u);
+            S.next_m = 0;
         }
         __syncthreads();
-        // Rounds of NT records: every lane runs the same alpha iteration at the
-        // same time (lanes without a record on this path are predicated off),
-        // so lanes never drift into different phases of the alpha loop.
-        const uint32_t r0 = cache.seg_off[w.m0], r1 = cache.seg_off[w.m1];
-        for (uint32_t base = r0; base < r1; base += NT) {
-            const uint32_t j = base + threadIdx.x;
-            uint32_t m = 0;
-            PairCtx c;
-            c.dinv = 0;
-            HotRec b{0.f, 0.f, 0u, 0u};
-            if (j < r1) {
-                m = cache.owner[j];
-                c = s_ctx[m - w.m0];
-                b = cache.hot[j];
-            }
-            const bool live = c.dinv != 0;
-            const bool cb = (b.rre & kCentralBit) != 0;
-            for (uint32_t k = 0; k < na; ++k) {
-                const HotRec a = s_alpha[k];
-                const bool ca = (a.rre & kCentralBit) != 0;
-                if (live && !(ca & cb)) {
-                    const bool two = !(ca | cb);
-                    acc.prod += two ? 2u : 1u;
-                    uint32_t st = eval_pair(a, b, two, c, s_tab, acc);
-                    if (st) {
-                        ExactRec ea = cache.exact[a0 + k], eb = cache.exact[j];
-                        resolve_exact(st, 2 * (__int128)ea.re, 2 * (__int128)ea.im, (__int128)eb.re,
-                                      (__int128)eb.im, w.l, m, cache.limit, w.row, s_tab, acc, buf);
-                    }
+        const uint32_t it = S.item;
+        if (it >= n_items) break;
+        const WorkItem w = items[it];
+        const RowInfo& R = buf.row_info[w.row];
+        const uint32_t a0 = R.seg, na = R.free_l + 1;
+        for (uint32_t i = tid; i < na; i += NT) scale2(cache.hot[a0 + i], s_alpha[i], s_abc[i]);
+        __syncthreads();
+        const uint32_t nm = w.m1 - w.m0;
+        for (;;) {
+            uint32_t c0 = 0;
+            if (lane == 0) c0 = atomicAdd(&S.next_m, 32u);
+            c0 = __shfl_sync(kFull, c0, 0);
+            if (c0 >= nm) break;
+            const uint32_t m = w.m0 + c0 + lane;
+            uint32_t kind = kSkip, s0 = 0, cnt = 0;
+            bool dual = false;
+            if (c0 + lane < nm) {
+                s0 = cache.seg_off[m];
+                const uint32_t s1 = cache.seg_off[m + 1];
+                kind = classify(R, m, s1 - s0 - 1);
+                if (kind == kCached) {
+                    uint32_t cc_c, cc_r;
+                    const PairCtx c = make_ctx(R, m, cc_c, cc_r);
+                    wctx[lane] = c;
+                    dual = pair_dual(c);
+                    cnt = s1 - s0;
+                    acc.processed += 1;
+                    acc.prod += 1;
+                    acc.cand += cc_c;
+                    acc.r16 += cc_r;
+                } else if (kind == kMerged) {
+                    acc.processed += 1;
+                    acc.merged += 1;
+                    push_merged(buf, w.l, m, w.row);
                 }
             }
+            __syncwarp();
+            batched_pass<false>(s_alpha, s_abc, na, wctx, dual ? 0u : cnt, s0, lane, cache, s_tab, a0, w.l, w.row,
+                                buf, q, qn, acc);
+            if (__any_sync(kFull, dual))
+                batched_pass<true>(s_alpha, s_abc, na, wctx, dual ? cnt : 0u, s0, lane, cache, s_tab, a0, w.l, w.row,
+                                   buf, q, qn, acc);
+            __syncwarp();
         }
         flush_acc(acc, &buf.rows[w.row]);
     }
@@ -625,25 +799,26 @@ __global__ void __launch_bounds__(NT, 512 / NT) batched_kernel(const DeviceCache
 
 // -------------------------------------------------------------- plain kernel
 
-__global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCache cache, uint64_t first_l,
-                                                              uint32_t alpha_cap, const LaunchBuffers buf) {
+// One block per (row, slice) and one thread per pair, as the reference
+// (gpu_search_v42.cu:298-304); events are handled by the lane that raised them.
+__global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCache cache, uint32_t alpha_cap,
+                                                                 const LaunchBuffers buf) {
     extern __shared__ __align__(16) unsigned char smem[];
-    HotRec* s_alpha = reinterpret_cast<HotRec*>(smem);
-    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_alpha + alpha_cap);
-    __shared__ RowConst s_row;
+    AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
+    uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_abc + alpha_cap);
     const uint32_t row = blockIdx.x / kSlices, slice = blockIdx.x % kSlices;
-    const uint64_t l = first_l + row;
+    const RowInfo& R = buf.row_info[row];
+    const uint64_t l = R.l;
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kPlainThreads) s_tab[i] = buf.tables[i];
-    if (threadIdx.x == 0) row_setup(cache, l, s_row);
-    const uint32_t a0 = cache.seg_off[l];
-    const uint32_t na = cache.seg_off[l + 1] - a0;
-    for (uint32_t i = threadIdx.x; i < na; i += kPlainThreads) s_alpha[i] = scale2(cache.hot[a0 + i]);
+    const uint32_t a0 = R.seg, na = R.free_l + 1;
+    for (uint32_t i = threadIdx.x; i < na; i += kPlainThreads) scale2(cache.hot[a0 + i], s_alpha[i], s_abc[i]);
     __syncthreads();
     Acc acc{0, 0, 0, 0, 0, 0};
     const uint64_t n = cache.limit;
     for (uint64_t m = l + slice * kPlainThreads + threadIdx.x; m <= n; m += kSlices * kPlainThreads) {
         const uint32_t s0 = cache.seg_off[m], s1 = cache.seg_off[m + 1];
-        const uint32_t kind = classify(s_row, cache, (uint32_t)m, s1 - s0 - 1);
+        const uint32_t kind = classify(R, (uint32_t)m, s1 - s0 - 1);
         if (kind == kSkip) continue;
         acc.processed += 1;
         if (kind == kMerged) {
@@ -652,26 +827,34 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
             continue;
         }
         uint32_t cc_c, cc_r;
-        const PairCtx c = make_ctx(s_row, m, cc_c, cc_r);
+        const PairCtx c = make_ctx(R, m, cc_c, cc_r);
         acc.prod += 1;
         acc.cand += cc_c;
         acc.r16 += cc_r;
         for (uint32_t j = s0; j < s1; ++j) {
             const HotRec b = cache.hot[j];
-            record_loop(s_alpha, na, b, c, s_tab, cache, a0, j, l, m, row, acc, buf);
+            const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+            const bool cb = (b.rre & kCentralBit) != 0;
+            for (uint32_t k = 0; k < na; ++k) {
+                const uint32_t flags = pair_dual(c) ? eval_fast<true>(s_alpha[k], b.re, b.im, bra, bia, cb, c, s_tab, acc)
+                                                    : eval_fast<false>(s_alpha[k], b.re, b.im, bra, bia, cb, c, s_tab, acc);
+                if (flags)
+                    add_event(acc, cached_event(flags, s_alpha[k], s_abc[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab,
+                                                (uint32_t)n, &buf));
+            }
         }
     }
     flush_acc(acc, &buf.rows[row]);
 }
 
-// ------------------------------------------------------------- merged kernel
+// ------------------------------------------------------------- merged kernels
 
 // Terms of a pair that shares split primes: merged exponents e = a + b
 // (gpu_search_v42.cu:318-338), split in two groups whose products form the
 // two lists; each list is the group's free set plus its central value.
 struct Group {
     uint32_t count;
-    uint32_t p[kMaxTerms], e[kMaxTerms];
+    uint32_t e[kMaxTerms];
     uint32_t base[kMaxTerms];   // index of the term's first value in the prime-power table
     uint32_t block[kMaxTerms];  // number of free vectors whose first non-central index is i
     uint32_t suffix[kMaxTerms]; // prod_{j>i} (4 e_j + 1)
@@ -709,9 +892,7 @@ __device__ void group_value(const DeviceCache& cache, const Group& g, uint32_t k
     } else {
         i = g.count;
     }
-    for (uint32_t j = 0; j < i; ++j) {  // central values of the leading terms: p^(2e), real
-        xr *= cache.pp_exact[2 * (g.base[j] + 2 * g.e[j])];
-    }
+    for (uint32_t j = 0; j < i; ++j) xr *= cache.pp_exact[2 * (g.base[j] + 2 * g.e[j])];
     if (i < g.count) {
         uint32_t r = k / g.suffix[i];
         uint32_t rem = k - r * g.suffix[i];
@@ -734,59 +915,66 @@ __device__ void group_value(const DeviceCache& cache, const Group& g, uint32_t k
     im = xi;
 }
 
-__device__ HotRec hot_of(i128 re, i128 im, bool central) {
-    HotRec h;
-    h.re = i128_to_float(re);
-    h.im = i128_to_float(im);
-    h.rre = pack_residues(re) | (central ? kCentralBit : 0u);
-    h.rim = pack_residues(im);
-    return h;
+__device__ void list_entry(i128 re, i128 im, bool central, AlphaHot& a, uint2& abc) {
+    uint32_t rw = pack_residues(re), iw = pack_residues(im);
+    a.re = i128_to_float(re);
+    a.im = i128_to_float(im);
+    a.ra = (rw & 1023u) | (central ? kCentralBit : 0u);
+    a.ia = iw & 1023u;
+    abc = make_uint2(rw, iw);
 }
 
-__device__ void merged_setup(const DeviceCache& cache, uint4 q, MergedShared& S, uint32_t list_cap) {
-    uint64_t l = q.x, m = q.y;
-    S.l = l;
+// One event of a shared-prime pair: list entries ka (alpha side) and kb.
+__device__ __forceinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc, AlphaHot bh, uint2 bbc,
+                                              PairCtx c, uint32_t ka, uint32_t kb, uint32_t l, uint32_t row,
+                                              const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf) {
+    Acc acc{0, 0, 0, 0, 0, 0};
+    const HotRec b{bh.re, bh.im, bbc.x | (bh.ra & kCentralBit), bbc.y};
+    process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
+                  [&](uint32_t kind) { push_exact(*buf, kind, ka, kb, l, pair_m(c), row, true); });
+    return make_uint2(acc.cand, acc.r16);
+}
+
+// Splits the merged terms of (l, m) into two groups (largest terms first,
+// each to the group with the smaller product of sizes).  ok = 1: fits
+// list_cap; 2: too big for it; 0: an exponent beyond the prime-power table.
+__device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, MergedShared& S,
+                             uint32_t list_cap) {
+    const uint64_t m = q.y;
+    S.l = q.x;
     S.m = m;
     S.row = q.z;
     S.ok = 1;
-    // factor l and m (split primes with exponents, and the fixed parts)
-    uint32_t lp[9], le[9], mp[9], me[9], nl = 0, nm = 0;
-    i128 fixed = 2;
-    for (int side = 0; side < 2; ++side) {
-        uint64_t x = side ? m : l;
-        uint32_t* P = side ? mp : lp;
-        uint32_t* E = side ? me : le;
-        uint32_t& cnt = side ? nm : nl;
-        while (x > 1) {
-            uint32_t p = cache.spf[x], a = 0;
-            do {
-                x /= p;
-                ++a;
-            } while (x % p == 0);
-            if ((p & 3u) == 1u) {
-                P[cnt] = p;
-                E[cnt] = a;
-                ++cnt;
-            } else {
-                for (uint32_t t = 0; t < 2 * a; ++t) fixed *= p;
-            }
+    uint32_t mp[9], me[9], nm = 0;
+    i128 fixed = (i128)2 * (i128)R.fixed;
+    uint64_t x = m;
+    while (x > 1) {
+        uint32_t p = cache.spf[x], a = 0;
+        do {
+            x /= p;
+            ++a;
+        } while (x % p == 0);
+        if ((p & 3u) == 1u) {
+            mp[nm] = p;
+            me[nm++] = a;
+        } else {
+            for (uint32_t t = 0; t < 2 * a; ++t) fixed *= p;
         }
     }
     uint32_t tp[kMaxTerms], te[kMaxTerms], count = 0;
     uint32_t i = 0, j = 0;
-    while (i < nl || j < nm) {
-        if (j == nm || (i < nl && lp[i] < mp[j])) {
-            tp[count] = lp[i];
-            te[count++] = le[i++];
-        } else if (i == nl || mp[j] < lp[i]) {
+    while (i < R.nsplit || j < nm) {
+        if (j == nm || (i < R.nsplit && R.sp[i] < mp[j])) {
+            tp[count] = R.sp[i];
+            te[count++] = R.se[i++];
+        } else if (i == R.nsplit || mp[j] < R.sp[i]) {
             tp[count] = mp[j];
             te[count++] = me[j++];
         } else {
-            tp[count] = lp[i];
-            te[count++] = le[i++] + me[j++];
+            tp[count] = R.sp[i];
+            te[count++] = R.se[i++] + me[j++];
         }
     }
-    // greedy split by list size: largest terms first, each to the smaller group
     uint32_t order[kMaxTerms];
     for (uint32_t t = 0; t < count; ++t) order[t] = t;
     for (uint32_t a = 1; a < count; ++a)
@@ -795,119 +983,55 @@ __device__ void merged_setup(const DeviceCache& cache, uint4 q, MergedShared& S,
             order[b] = order[b - 1];
             order[b - 1] = tmp;
         }
-    uint64_t w[2] = {1, 1};
+    uint64_t wsz[2] = {1, 1};
     S.g[0].count = S.g[1].count = 0;
     for (uint32_t t = 0; t < count; ++t) {
         uint32_t idx = order[t];
-        int side = w[0] <= w[1] ? 0 : 1;
+        int side = wsz[0] <= wsz[1] ? 0 : 1;
         Group& g = S.g[side];
-        g.p[g.count] = tp[idx];
         g.e[g.count] = te[idx];
         g.base[g.count] = cache.pp_base[tp[idx]] + pp_exponent_offset(te[idx]);
         ++g.count;
-        w[side] *= 4 * te[idx] + 1;
+        wsz[side] *= 4 * te[idx] + 1;
         if (te[idx] > cache.max_exponent) S.ok = 0;
     }
     group_finish(S.g[0]);
     group_finish(S.g[1]);
     S.g[0].scale = fixed;
     S.g[1].scale = 1;
-    if (S.g[0].free_count + S.g[1].free_count + 2 > list_cap) S.ok = 2;  // too big for this path
+    if (S.ok == 1 && S.g[0].free_count + S.g[1].free_count + 2 > list_cap) S.ok = 2;
 }
 
-__global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ MergedShared S;
-    __shared__ __align__(16) HotRec s_list[kMergedListCap];
-    __shared__ uint8_t s_tab[kTableBytes];
-    __shared__ RowConst s_row;
-    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
-    const uint32_t count = min(*buf.big_count, buf.big_cap);
-    for (uint32_t q = blockIdx.x; q < count; q += gridDim.x) {
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint4 e = buf.big_queue[q];
-            merged_setup(cache, e, S, kMergedListCap);
-            row_setup(cache, e.x, s_row);
-            uint32_t cc_c, cc_r;
-            S.ctx = make_ctx(s_row, e.y, cc_c, cc_r);
-            S.cc_cand = cc_c;
-            S.cc_r16 = cc_r;
-            if (S.ok != 1) atomicOr(buf.error_flags, 2u);
-        }
-        __syncthreads();
-        if (S.ok != 1) continue;
-        const uint32_t na = S.g[0].free_count + 1, nb = S.g[1].free_count + 1;
-        HotRec* s_a = s_list;
-        HotRec* s_b = s_list + na;
-        for (uint32_t k = threadIdx.x; k < na + nb; k += kMergedThreads) {
-            int side = k < na ? 0 : 1;
-            uint32_t idx = side ? k - na : k;
-            i128 re, im;
-            group_value(cache, S.g[side], idx, re, im);
-            s_list[k] = hot_of(re, im, idx == S.g[side].free_count);
-        }
-        __syncthreads();
-        Acc acc{0, 0, 0, 0, 0, 0};
-        if (threadIdx.x == 0) {
-            acc.prod += 1;
-            acc.cand += S.cc_cand;
-            acc.r16 += S.cc_r16;
-        }
-        const uint32_t total = na * nb;
-        const float rcp = 1.0f / (float)nb;
-        for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
-            uint32_t ka = (uint32_t)((float)k * rcp);
-            int32_t kb = (int32_t)(k - ka * nb);
-            while (kb < 0) {
-                --ka;
-                kb += (int32_t)nb;
-            }
-            while (kb >= (int32_t)nb) {
-                ++ka;
-                kb -= (int32_t)nb;
-            }
-            const HotRec a = s_a[ka], b = s_b[kb];
-            const bool ca = (a.rre & kCentralBit) != 0, cb = (b.rre & kCentralBit) != 0;
-            if (ca & cb) continue;
-            const bool two = !(ca | cb);
-            acc.prod += two ? 2u : 1u;
-            uint32_t st = eval_pair(a, b, two, S.ctx, s_tab, acc);
-            if (st) {
-                i128 ar, ai, br, bi;
-                group_value(cache, S.g[0], ka, ar, ai);
-                group_value(cache, S.g[1], (uint32_t)kb, br, bi);
-                resolve_exact(st, ar, ai, br, bi, S.l, S.m, cache.limit, S.row, s_tab, acc, buf);
-            }
-        }
-        flush_acc(acc, &buf.rows[S.row], true);
-    }
-}
-
-// Shared-prime pairs, one warp per pair: lane 0 factors the pair and splits
-// its terms, the lanes build both lists in the warp's shared slice, then all
-// (alpha, beta) combinations are evaluated in lockstep rounds of 32.  Pairs
-// whose lists exceed the slice go to the big-pair queue (one CTA per pair).
+// Shared-prime pairs, one warp per pair: lane 0 factors m and splits the
+// terms, the lanes build both lists in the warp's shared slice, then all
+// (alpha, beta) combinations are evaluated in lockstep rounds of 32 with a
+// warp event queue.  Pairs whose lists exceed the slice go to the big-pair
+// queue (one CTA per pair).
 __global__ void __launch_bounds__(kWarpPairThreads, 2) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
     __shared__ MergedShared S[kWarpPairWarps];
-    __shared__ RowConst R[kWarpPairWarps];
-    __shared__ __align__(16) HotRec s_list[kWarpPairWarps][kWarpListCap];
+    __shared__ __align__(16) AlphaHot s_list[kWarpPairWarps][kWarpListCap];
+    __shared__ uint2 s_lbc[kWarpPairWarps][kWarpListCap];
+    __shared__ uint64_t s_queue[kWarpPairWarps][kQueue];
     __shared__ uint8_t s_tab[kTableBytes];
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kWarpPairThreads) s_tab[i] = buf.tables[i];
     __syncthreads();
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
     MergedShared& P = S[warp];
-    HotRec* list = s_list[warp];
+    AlphaHot* list = s_list[warp];
+    uint2* lbc = s_lbc[warp];
+    uint64_t* q = s_queue[warp];
+    uint32_t qn = 0;
     const uint32_t count = min(*buf.merged_count, buf.merged_cap);
     const uint32_t stride = gridDim.x * kWarpPairWarps;
-    for (uint32_t q = blockIdx.x * kWarpPairWarps + warp; q < count; q += stride) {
+    for (uint32_t qi = blockIdx.x * kWarpPairWarps + warp; qi < count; qi += stride) {
         __syncwarp();
+        const uint4 e = buf.merged_queue[qi];
+        const RowInfo& R = buf.row_info[e.z];
         if (lane == 0) {
-            uint4 e = buf.merged_queue[q];
-            merged_setup(cache, e, P, kWarpListCap);
+            merged_setup(cache, R, e, P, kWarpListCap);
             if (P.ok == 1) {
-                row_setup(cache, e.x, R[warp]);
                 uint32_t cc_c, cc_r;
-                P.ctx = make_ctx(R[warp], e.y, cc_c, cc_r);
+                P.ctx = make_ctx(R, e.y, cc_c, cc_r);
                 P.cc_cand = cc_c;
                 P.cc_r16 = cc_r;
             } else if (P.ok == 2) {
@@ -924,11 +1048,11 @@ __global__ void __launch_bounds__(kWarpPairThreads, 2) merged_kernel(const Devic
         if (P.ok != 1) continue;
         const uint32_t na = P.g[0].free_count + 1, nb = P.g[1].free_count + 1;
         for (uint32_t k = lane; k < na + nb; k += 32) {
-            int side = k < na ? 0 : 1;
-            uint32_t idx = side ? k - na : k;
-            __int128 re, im;
+            const int side = k < na ? 0 : 1;
+            const uint32_t idx = side ? k - na : k;
+            i128 re, im;
             group_value(cache, P.g[side], idx, re, im);
-            list[k] = hot_of(re, im, idx == P.g[side].free_count);
+            list_entry(re, im, idx == P.g[side].free_count, list[k], lbc[k]);
         }
         __syncwarp();
         Acc acc{0, 0, 0, 0, 0, 0};
@@ -940,42 +1064,139 @@ __global__ void __launch_bounds__(kWarpPairThreads, 2) merged_kernel(const Devic
         const PairCtx c = P.ctx;
         const uint32_t total = na * nb;
         const float rcp = 1.0f / (float)nb;
+        auto handle = [&](uint64_t ev) {
+            const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+            add_event(acc, merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c, ka, kb,
+                                        (uint32_t)P.l, P.row, s_tab, (uint32_t)cache.limit, &buf));
+        };
         for (uint32_t base = 0; base < total; base += 32) {
             const uint32_t k = base + lane;
-            uint32_t ka = (uint32_t)((float)k * rcp);
-            int32_t kb = (int32_t)k - (int32_t)(ka * nb);
-            while (kb < 0) {
-                --ka;
-                kb += (int32_t)nb;
-            }
-            while (kb >= (int32_t)nb) {
-                ++ka;
-                kb -= (int32_t)nb;
-            }
+            uint32_t flags = 0, ka = 0;
+            int32_t kb = 0;
             if (k < total) {
-                const HotRec a = list[ka], b = list[na + kb];
-                const bool ca = (a.rre & kCentralBit) != 0, cb = (b.rre & kCentralBit) != 0;
-                if (!(ca & cb)) {
-                    const bool two = !(ca | cb);
-                    acc.prod += two ? 2u : 1u;
-                    uint32_t st = eval_pair(a, b, two, c, s_tab, acc);
-                    if (st) {
-                        __int128 ar, ai, br, bi;
-                        group_value(cache, P.g[0], ka, ar, ai);
-                        group_value(cache, P.g[1], (uint32_t)kb, br, bi);
-                        resolve_exact(st, ar, ai, br, bi, P.l, P.m, cache.limit, P.row, s_tab, acc, buf);
-                    }
+                ka = (uint32_t)((float)k * rcp);
+                kb = (int32_t)k - (int32_t)(ka * nb);
+                while (kb < 0) {
+                    --ka;
+                    kb += (int32_t)nb;
                 }
+                while (kb >= (int32_t)nb) {
+                    ++ka;
+                    kb -= (int32_t)nb;
+                }
+                const AlphaHot a = list[ka], bh = list[na + kb];
+                flags = pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c,
+                                                       s_tab, acc)
+                                     : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
+                                                        c, s_tab, acc);
             }
+            if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags))) drain(q, qn, 32, handle);
         }
+        while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
         flush_acc(acc, &buf.rows[P.row], true);
     }
 }
 
+// Shared-prime pairs too big for a warp: one CTA per pair, events handled by
+// the lane that raised them.
+__global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+    __shared__ MergedShared S;
+    __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
+    __shared__ uint2 s_lbc[kMergedListCap];
+    __shared__ uint8_t s_tab[kTableBytes];
+    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
+    const uint32_t count = min(*buf.big_count, buf.big_cap);
+    for (uint32_t qi = blockIdx.x; qi < count; qi += gridDim.x) {
+        __syncthreads();
+        const uint4 e = buf.big_queue[qi];
+        const RowInfo& R = buf.row_info[e.z];
+        if (threadIdx.x == 0) {
+            merged_setup(cache, R, e, S, kMergedListCap);
+            uint32_t cc_c, cc_r;
+            S.ctx = make_ctx(R, e.y, cc_c, cc_r);
+            S.cc_cand = cc_c;
+            S.cc_r16 = cc_r;
+            if (S.ok != 1) atomicOr(buf.error_flags, 2u);
+        }
+        __syncthreads();
+        if (S.ok != 1) continue;
+        const uint32_t na = S.g[0].free_count + 1, nb = S.g[1].free_count + 1;
+        for (uint32_t k = threadIdx.x; k < na + nb; k += kMergedThreads) {
+            const int side = k < na ? 0 : 1;
+            const uint32_t idx = side ? k - na : k;
+            i128 re, im;
+            group_value(cache, S.g[side], idx, re, im);
+            list_entry(re, im, idx == S.g[side].free_count, s_list[k], s_lbc[k]);
+        }
+        __syncthreads();
+        Acc acc{0, 0, 0, 0, 0, 0};
+        if (threadIdx.x == 0) {
+            acc.prod += 1;
+            acc.cand += S.cc_cand;
+            acc.r16 += S.cc_r16;
+        }
+        const PairCtx c = S.ctx;
+        const uint32_t total = na * nb;
+        for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
+            const uint32_t ka = k / nb, kb = k - ka * nb;
+            const AlphaHot a = s_list[ka], bh = s_list[na + kb];
+            const uint32_t flags =
+                pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
+                             : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c, s_tab,
+                                                acc);
+            if (flags)
+                add_event(acc, merged_event(flags, a, s_lbc[ka], bh, s_lbc[na + kb], c, ka, kb, (uint32_t)S.l, S.row,
+                                            s_tab, (uint32_t)cache.limit, &buf));
+        }
+        flush_acc(acc, &buf.rows[S.row], true);
+    }
+}
+
+// Exact work queued by the search kernels (rare: products whose window
+// decision was within the float error bound, and possible hits).  Exact
+// coordinates come from the cache (row values doubled) or, for pairs that
+// share a split prime, from the two term groups rebuilt for the pair.
+__global__ void __launch_bounds__(128) exact_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+    __shared__ uint8_t s_tab[kTableBytes];
+    for (uint32_t i = threadIdx.x; i < kTableBytes; i += blockDim.x) s_tab[i] = buf.tables[i];
+    __syncthreads();
+    const uint32_t count = min(*buf.exact_count, buf.exact_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const ExactItem it = buf.exact_queue[i];
+        const uint32_t kind = it.kind & 3u, p = (it.kind >> 2) & 1u, o = (it.kind >> 3) & 1u;
+        const bool shared_prime = (it.kind & 16u) != 0;
+        i128 ar, ai, br, bi;
+        if (shared_prime) {
+            MergedShared S;
+            merged_setup(cache, buf.row_info[it.row], make_uint4(it.l, it.m, it.row, 0u), S, 0xFFFFFFFFu);
+            group_value(cache, S.g[0], it.a, ar, ai);
+            group_value(cache, S.g[1], it.b, br, bi);
+        } else {
+            const ExactRec ea = cache.exact[it.a], eb = cache.exact[it.b];
+            ar = 2 * (i128)ea.re;
+            ai = 2 * (i128)ea.im;
+            br = eb.re;
+            bi = eb.im;
+        }
+        const uint32_t omask = kind == kExCount ? 3u : (o ? 2u : 1u);
+        uint32_t c = 0, r = 0;
+        exact_eval(ar, ai, br, bi, p == 1, omask, it.l, it.m, cache.limit, it.row, s_tab, buf, &c, &r);
+        if (kind != kExHit) {
+            RowCounts* rc = &buf.rows[it.row];
+            atomicAdd(&rc->candidates, (unsigned long long)c);
+            atomicAdd(&rc->r16, (unsigned long long)r);
+            atomicAdd(&rc->exact, 1ull);
+            if (shared_prime) {
+                atomicAdd(&rc->mcandidates, (unsigned long long)c);
+                atomicAdd(&rc->mr16, (unsigned long long)r);
+            }
+        }
+    }
+}
+
 // INT32 throughput probe: 8 independent chains per thread, each step one
-// IMAD and one LOP3 (the multiply and logic pipes the search loop uses),
-// i.e. 16 integer instructions per unrolled step; the result is stored so
-// nothing is eliminated.
+// IMAD and one shift/logic pair (the multiply and logic pipes the search loop
+// uses); the result is stored so nothing is eliminated.
 __global__ void __launch_bounds__(256) int_peak_kernel(uint32_t iters, uint32_t seed, uint32_t* out) {
     uint32_t a[8];
 #pragma unroll
@@ -1015,12 +1236,50 @@ double int32_peak_ops(int device, int sm_count, double* ms_out) {
     cudaEventDestroy(e1);
     cudaFree(out);
     if (ms_out) *ms_out = ms;
-    // per unrolled step: 8 IMAD + 8 shift-xor-and (SHF/LOP3 pairs count as 2)
+    // per unrolled step: 8 chains x (IMAD + SHF + LOP3)
     double ops = (double)blocks * threads * iters * 8.0 * 3.0;
     return ms > 0 ? ops / (ms * 1e-3) : 0;
 }
 
 // ------------------------------------------------------------------ host side
+
+void fill_row_info(const uint32_t* spf, const uint32_t* seg_off, uint64_t n, uint64_t l, RowInfo* R) {
+    *R = RowInfo{};
+    R->l = l;
+    R->l2 = l * l;
+    R->l4 = (u128)R->l2 * R->l2;
+    R->n4 = (u128)(n * n) * (n * n);
+    R->lmodA = mod_u128_small(R->l4, kModA);
+    R->lmodB = mod_u128_small(R->l4, kModB);
+    R->lmodC = mod_u128_small(R->l4, kModC);
+    R->l2modA = (uint32_t)(R->l2 % kModA);
+    R->l3 = l % 3 == 0;
+    R->l5 = l % 5 == 0;
+    R->leven = (l & 1) == 0;
+    R->free_l = seg_off[l + 1] - seg_off[l] - 1;
+    R->seg = seg_off[l];
+    R->fixed = 1;
+    uint64_t x = l;
+    while (x > 1) {
+        uint32_t p = spf[x], a = 0;
+        do {
+            x /= p;
+            ++a;
+        } while (x % p == 0);
+        if ((p & 3u) == 1u) {
+            R->sp[R->nsplit] = p;
+            R->se[R->nsplit] = a;
+            ++R->nsplit;
+        } else {
+            for (uint32_t t = 0; t < 2 * a; ++t) R->fixed *= p;
+        }
+        if (p == 2) continue;
+        R->pinv[R->nodd] = inverse_odd(p);
+        R->pthr[R->nodd] = 0xFFFFFFFFu / p;
+        if ((p & 3u) == 1u) R->psplit |= 1u << R->nodd;
+        ++R->nodd;
+    }
+}
 
 void build_residue_tables(uint8_t* out) {
     auto is4 = [](uint32_t r, uint32_t m) {
@@ -1040,20 +1299,22 @@ void build_residue_tables(uint8_t* out) {
         out[kTabC + z] = (is4(z % 7, 7) && is4(z % 13, 13) && is4(z % 17, 17)) ? 1 : 0;
 }
 
-size_t batched_smem_bytes(uint32_t alpha_cap, uint32_t tile_cap) {
-    return (size_t)alpha_cap * sizeof(HotRec) + (size_t)tile_cap * sizeof(PairCtx) + kTableBytes;
+size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
+    const uint32_t warps = (uint32_t)threads / 32;
+    return (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) + (size_t)warps * 32 * sizeof(PairCtx) +
+           (size_t)warps * kQueue * sizeof(uint64_t) + kTableBytes;
 }
 
-static const void* batched_fn(int threads) {
-    switch (threads) {
-        case 128: return (const void*)batched_kernel<128>;
-        case 512: return (const void*)batched_kernel<512>;
-        default: return (const void*)batched_kernel<256>;
-    }
+// Compiled (threads, min CTAs per SM) variants of the persistent kernel; the
+// second number caps registers per thread (65536 / (threads * min)).
+static const void* batched_fn(int threads, int min_blocks) {
+    if (threads == 128) return min_blocks >= 6 ? (const void*)batched_kernel<128, 6> : (const void*)batched_kernel<128, 4>;
+    if (threads == 512) return (const void*)batched_kernel<512, 1>;
+    return min_blocks >= 3 ? (const void*)batched_kernel<256, 3> : (const void*)batched_kernel<256, 2>;
 }
 
-int batched_max_ctas_per_sm(int threads, size_t smem) {
-    const void* fn = batched_fn(threads);
+int batched_max_ctas_per_sm(int threads, int min_blocks, size_t smem) {
+    const void* fn = batched_fn(threads, min_blocks);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem) != cudaSuccess) return 1;
@@ -1062,31 +1323,22 @@ int batched_max_ctas_per_sm(int threads, size_t smem) {
 
 cudaError_t launch_batched(const DeviceCache& cache, const WorkItem* items, uint32_t n_items,
                            const BatchedConfig& cfg, const LaunchBuffers& buf, cudaStream_t stream) {
-    size_t smem = batched_smem_bytes(cfg.alpha_cap, cfg.tile_cap);
-    const void* fn = batched_fn(cfg.threads);
+    size_t smem = batched_smem_bytes(cfg.threads, cfg.alpha_cap);
+    const void* fn = batched_fn(cfg.threads, cfg.min_blocks);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    switch (cfg.threads) {
-        case 128:
-            batched_kernel<128><<<cfg.ctas, 128, smem, stream>>>(cache, items, n_items, cfg.alpha_cap, cfg.tile_cap, buf);
-            break;
-        case 512:
-            batched_kernel<512><<<cfg.ctas, 512, smem, stream>>>(cache, items, n_items, cfg.alpha_cap, cfg.tile_cap, buf);
-            break;
-        default:
-            batched_kernel<256><<<cfg.ctas, 256, smem, stream>>>(cache, items, n_items, cfg.alpha_cap, cfg.tile_cap, buf);
-            break;
-    }
-    return cudaGetLastError();
+    void* args[] = {(void*)&cache, (void*)&items, (void*)&n_items, (void*)&cfg.alpha_cap, (void*)&buf};
+    return cudaLaunchKernel(fn, dim3(cfg.ctas), dim3(cfg.threads), args, smem, stream);
 }
 
 cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_rows, uint32_t alpha_cap,
                          const LaunchBuffers& buf, cudaStream_t stream) {
-    size_t smem = (size_t)alpha_cap * sizeof(HotRec) + kTableBytes;
+    (void)first_l;
+    size_t smem = (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) + kTableBytes;
     cudaError_t e = cudaFuncSetAttribute((const void*)plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    plain_kernel<<<n_rows * kSlices, kPlainThreads, smem, stream>>>(cache, first_l, alpha_cap, buf);
+    plain_kernel<<<n_rows * kSlices, kPlainThreads, smem, stream>>>(cache, alpha_cap, buf);
     return cudaGetLastError();
 }
 
@@ -1097,6 +1349,11 @@ cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const Launch
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     merged_big_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_exact(const DeviceCache& cache, const LaunchBuffers& buf, int ctas, cudaStream_t stream) {
+    exact_kernel<<<ctas, 128, 0, stream>>>(cache, buf);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,32 @@ namespace hss {
 constexpr uint32_t kTableBytes = 720 + 625 + 1547;
 void build_residue_tables(uint8_t* out /* kTableBytes */);
 
+// Constants of one root row, built on the host for every row of a launch
+// (so no kernel factors l): l, l^2, l^4, N^4, residues, the odd primes of l
+// as divisibility constants (m * inv <= thr exactly when p | m), and the split
+// primes of l for the shared-prime path.
+struct RowInfo {
+    uint64_t l, l2;
+    unsigned __int128 l4, n4;
+    uint64_t fixed;             // prod of non-split p^(2a) of l
+    uint32_t lmodA, lmodB, lmodC, l2modA;  // l^4 mod 720, 625, 1547; l^2 mod 720
+    uint32_t l3, l5, leven, nodd;          // 3 | l, 5 | l, l even, number of odd primes
+    uint32_t pinv[9], pthr[9];
+    uint32_t psplit;            // bit i set when odd prime i is = 1 mod 4
+    uint32_t free_l, seg;       // |free(l)| and the first record of l's segment
+    uint32_t nsplit;            // split primes of l (increasing) with exponents
+    uint32_t sp[8], se[8];
+    uint32_t pad;
+};
+
+// Exact work queued by the search kernels for exact_kernel: kind bits 0-1
+// (0: count a whole product, 1: count one orientation, 2: hit test of one
+// orientation), bit 2: product alpha*conj(beta), bit 3: orientation (y, x),
+// bit 4: shared-prime pair (a, b are list entries rather than cache indices).
+struct ExactItem {
+    uint32_t kind, a, b, l, m, row, pad0, pad1;
+};
+
 // Device buffers one search call writes.
 struct LaunchBuffers {
     RowCounts* rows;            // [n_rows]
@@ -25,22 +51,35 @@ struct LaunchBuffers {
     unsigned int* merged_count; // entries appended (may exceed merged_cap)
     uint32_t merged_cap;
     unsigned int* next_item;    // work-queue cursor of the batched kernel
-    unsigned int* error_flags;  // bit 0: shared-prime queue full; bit 1: pair lists over capacity
+    unsigned int* error_flags;  // bit 0: shared-prime queue full; 1: pair lists over capacity; 2: exact queue full
     uint4* big_queue;           // shared-prime pairs too big for one warp's lists
     unsigned int* big_count;
     uint32_t big_cap;
     const uint8_t* tables;      // kTableBytes residue tables
+    const RowInfo* row_info;    // [n_rows] constants of the launch's rows
+    ExactItem* exact_queue;     // rare exact work (undecided products, possible hits)
+    unsigned int* exact_count;
+    uint32_t exact_cap;
 };
+
+// Host-side fill of a RowInfo from the smallest-prime-factor table.
+void fill_row_info(const uint32_t* spf, const uint32_t* seg_off, uint64_t limit, uint64_t l, RowInfo* out);
 
 struct BatchedConfig {
-    int threads;        // CTA size
+    int threads;        // CTA size (128, 256 or 512)
+    int min_blocks;     // compiled minimum CTAs per SM (register cap): 128 -> 4|6, 256 -> 2|3, 512 -> 1
     int ctas;           // persistent grid size
     uint32_t alpha_cap; // largest row segment (free set + centre) among items
-    uint32_t tile_cap;  // largest m-range among items
 };
 
+// The batched kernel walks an item's m-range in sub-tiles of at most
+// `threads` roots and kItemRecords m-side records (the compacted record list
+// lives in shared memory), so one root's segment must fit kItemRecords.
+constexpr uint32_t kItemRecords = 4096;
+inline uint32_t tile_cap_for(int threads) { return (uint32_t)threads; }
+
 // Shared memory the batched kernel needs for a configuration.
-size_t batched_smem_bytes(uint32_t alpha_cap, uint32_t tile_cap);
+size_t batched_smem_bytes(int threads, uint32_t alpha_cap);
 
 // Persistent kernel over work items (row l, m in [m0, m1)).
 cudaError_t launch_batched(const DeviceCache& cache, const WorkItem* items, uint32_t n_items,
@@ -58,7 +97,10 @@ cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const Launch
 // Integer-op throughput of the device measured by a probe kernel (ops/s).
 double int32_peak_ops(int device, int sm_count, double* ms);
 
+// Exact work queued by the search kernels; run after them.
+cudaError_t launch_exact(const DeviceCache& cache, const LaunchBuffers& buf, int ctas, cudaStream_t stream);
+
 // Occupancy helper for the persistent grid.
-int batched_max_ctas_per_sm(int threads, size_t smem);
+int batched_max_ctas_per_sm(int threads, int min_blocks, size_t smem);
 
 }  // namespace hss

@@ -55,6 +55,11 @@ class HssHit(ctypes.Structure):
         return abs(area4) // 4
 
 
+class HssTuneTrial(ctypes.Structure):
+    _fields_ = [("block_threads", ctypes.c_uint32), ("ctas_per_sm", ctypes.c_uint32),
+                ("item_target", ctypes.c_uint32), ("ms", ctypes.c_float)]
+
+
 class HssRequestInfo(ctypes.Structure):
     _fields_ = [("first", ctypes.c_uint64), ("last", ctypes.c_uint64),
                 ("submitted_ns", ctypes.c_uint64), ("admitted_ns", ctypes.c_uint64),
@@ -91,6 +96,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                p(u32)]
     lib.hss_search_many.argtypes = [ctypes.c_void_p, p(u64), p(u64), u32, p(HssCounts),
                                     p(HssCounts), p(HssHit), u32, p(u32)]
+    lib.hss_autotune.argtypes = [ctypes.c_void_p, u64, u64, p(HssOpts), p(HssTuneTrial), u32, p(u32)]
     lib.hss_serve_start.argtypes = [ctypes.c_void_p, u32, u32]
     lib.hss_submit.argtypes = [ctypes.c_void_p, u64, u64, p(u64)]
     lib.hss_poll.argtypes = [ctypes.c_void_p, u64, p(HssRequestInfo), p(HssHit), u32]
@@ -187,6 +193,17 @@ class Search:
                                              hits, hit_cap, ctypes.byref(nh)))
         h, ok = _hits(hits, min(nh.value, hit_cap))
         return [p.as_dict() for p in per], SearchResult(total.as_dict(), h, ok)
+
+    def autotune(self, first: int, last: int):
+        """Times every kernel variant and item weight on rows first..last and
+        keeps the fastest; returns (chosen options, trials)."""
+        best = HssOpts()
+        trials = (HssTuneTrial * 64)()
+        n = ctypes.c_uint32()
+        self._check(self.lib.hss_autotune(self.handle, first, last, ctypes.byref(best), trials, 64,
+                                          ctypes.byref(n)))
+        chosen = {name: getattr(best, name) for name, _ in best._fields_}
+        return chosen, [(t.block_threads, t.ctas_per_sm, t.item_target, t.ms) for t in trials[:n.value]]
 
     # -- serving
     def serve_start(self, max_active: int = 0, wave_mpairs: int = 0):

@@ -36,7 +36,7 @@ extern "C" {
 #define HSS_ERR_BUSY (-8)      /* request still running */
 #define HSS_ERR_NO_DEVICE (-9) /* no CUDA device / wrong architecture */
 
-#define HSS_MAX_LIMIT 100000000ULL
+#define HSS_MAX_LIMIT 30000000ULL  /* every segment (<= 4063 values) fits a work item */
 
 /* Enumeration paths.  PLAIN mirrors the reference's launch shape (one block
  * per (root, slice), one thread per pair, gpu_search_v42.cu:298-304);
@@ -54,7 +54,9 @@ typedef struct {
     uint32_t block_threads;   /* batched CTA size: 128, 256 or 512 (0: 256) */
     uint32_t item_target;     /* batched item weight in alpha*beta evaluations
                                  (0: 1<<20) */
-    uint32_t ctas_per_sm;     /* persistent CTAs per SM (0: from occupancy) */
+    uint32_t ctas_per_sm;     /* batched kernel variant: minimum CTAs per SM it is
+                                 compiled for (128 threads: 4 or 6; 256: 2 or 3;
+                                 512: 1); 0 picks 6 / 3 / 1 */
     uint32_t use_graph;       /* 1: capture each batched launch sequence in a
                                  CUDA graph */
 } hss_opts;
@@ -142,6 +144,20 @@ int hss_cache_inspect(uint64_t limit, uint64_t x, uint64_t* records, uint64_t* f
  * *nhits receives the number found (which may exceed hit_cap). */
 int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* out,
                uint64_t* row_candidates, hss_hit* hits, uint32_t hit_cap, uint32_t* nhits);
+
+/* Autotuner: times the batched path on rows first..last (a sample of the
+ * intended workload) for every compiled kernel variant (CTA size and minimum
+ * CTAs per SM, which caps registers per thread) and item weight, keeps the
+ * fastest configuration in the handle's options and returns it in *best.
+ * `trials` receives up to max_trials (threads, ctas_per_sm, item_target,
+ * milliseconds) records when not NULL. */
+typedef struct {
+    uint32_t block_threads, ctas_per_sm, item_target;
+    float ms;
+} hss_tune_trial;
+
+int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tune_trial* trials,
+                 uint32_t max_trials, uint32_t* ntrials);
 
 /* Batched search of several intervals in one persistent launch sequence:
  * intervals i = [firsts[i], lasts[i]].  per_interval (count entries) receives
