@@ -532,12 +532,16 @@ __device__ __forceinline__ uint32_t classify(const RowInfo& R, uint32_t m, uint3
 // the all-central product (2 l^2 m^2, 0), whose only orientation with a
 // nonzero area is D = 0, 4A = 2 l^2 m^2 (counted when the window contains 0;
 // z = l^4 + m^4 is never a fourth power).
-__device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16) {
+// eps_scale: 2^-20 for values read from the cache (float coordinates within
+// 2^-24 relative, products within 4 * 2^-24 of |z|), 2^-16 for shared-prime
+// lists multiplied out in float (at most 16 factors: within 71 * 2^-24).
+__device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16,
+                           float eps_scale = 0x1p-20f) {
     uint64_t m2 = m * m;
     u128 m4 = (u128)m2 * m2;
     i128 w = (i128)R.l4 + (i128)m4 - (i128)R.n4;
     u128 twoL = (u128)(2 * R.l2) * m2;
-    float E = u128_to_float(twoL) * 0x1p-20f;
+    float E = u128_to_float(twoL) * eps_scale;
     float T2 = u128_to_float(R.l4);
     float e2 = E + T2 * 0x1p-22f;
     float wf = i128_to_float(w);
@@ -860,6 +864,8 @@ struct Group {
     uint32_t suffix[kMaxTerms]; // prod_{j>i} (4 e_j + 1)
     uint32_t free_count;
     i128 scale;                 // real factor folded into every value of the group
+    float scale_f;              // the same as float and packed residues
+    uint32_t scale_res;
 };
 
 struct MergedShared {
@@ -913,6 +919,68 @@ __device__ void group_value(const DeviceCache& cache, const Group& g, uint32_t k
     }
     re = xr;
     im = xi;
+}
+
+// Complex product of packed residues (mod 720 | 625 << 10 | 1547 << 20).
+__device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, uint32_t bi, uint32_t& xr,
+                                        uint32_t& xi) {
+    uint32_t outr = 0, outi = 0;
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+        const uint32_t shift = f == 0 ? 0u : (f == 1 ? 10u : 20u);
+        const uint32_t mask = f == 2 ? 2047u : 1023u;
+        const uint32_t M = f == 0 ? kModA : (f == 1 ? kModB : kModC);
+        const uint32_t a0 = (ar >> shift) & mask, a1 = (ai >> shift) & mask;
+        const uint32_t b0 = (br >> shift) & mask, b1 = (bi >> shift) & mask;
+        outr |= ((a0 * b0 + M * M - a1 * b1) % M) << shift;
+        outi |= ((a0 * b1 + a1 * b0) % M) << shift;
+    }
+    xr = outr;
+    xi = outi;
+}
+
+// List entry k of group g multiplied out in float and residues (the same
+// decode as group_value; the exact value is rebuilt only for exact work).
+__device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32_t k, AlphaHot& out, uint2& abc) {
+    float xr = g.scale_f, xi = 0.f;
+    uint32_t rr = g.scale_res, ri = 0u;
+    uint32_t i = 0;
+    const bool central = k >= g.free_count;
+    if (!central) {
+        while (k >= g.block[i]) {
+            k -= g.block[i];
+            ++i;
+        }
+    } else {
+        i = g.count;
+    }
+    auto mul = [&](const HotRec& v) {
+        const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
+        uint32_t yr, yi;
+        res_mul(rr, ri, v.rre & 0x7FFFFFFFu, v.rim, yr, yi);
+        xr = nr;
+        xi = ni;
+        rr = yr;
+        ri = yi;
+    };
+    for (uint32_t j = 0; j < i; ++j) mul(cache.pp_hot[g.base[j] + 2 * g.e[j]]);
+    if (i < g.count) {
+        uint32_t r = k / g.suffix[i];
+        uint32_t rem = k - r * g.suffix[i];
+        uint32_t digits[kMaxTerms];
+        for (uint32_t j = g.count - 1; j > i; --j) {
+            uint32_t s = 4 * g.e[j] + 1;
+            digits[j] = rem % s;
+            rem /= s;
+        }
+        digits[i] = r;
+        for (uint32_t j = i; j < g.count; ++j) mul(cache.pp_hot[g.base[j] + digits[j]]);
+    }
+    out.re = xr;
+    out.im = xi;
+    out.ra = (rr & 1023u) | (central ? kCentralBit : 0u);
+    out.ia = ri & 1023u;
+    abc = make_uint2(rr, ri);
 }
 
 __device__ void list_entry(i128 re, i128 im, bool central, AlphaHot& a, uint2& abc) {
@@ -999,101 +1067,205 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
     group_finish(S.g[1]);
     S.g[0].scale = fixed;
     S.g[1].scale = 1;
+    S.g[0].scale_f = i128_to_float(fixed);
+    S.g[0].scale_res = pack_residues(fixed);
+    S.g[1].scale_f = 1.f;
+    S.g[1].scale_res = 1u | (1u << 10) | (1u << 20);
     if (S.ok == 1 && S.g[0].free_count + S.g[1].free_count + 2 > list_cap) S.ok = 2;
 }
 
-// Shared-prime pairs, one warp per pair: lane 0 factors m and splits the
-// terms, the lanes build both lists in the warp's shared slice, then all
-// (alpha, beta) combinations are evaluated in lockstep rounds of 32 with a
-// warp event queue.  Pairs whose lists exceed the slice go to the big-pair
-// queue (one CTA per pair).
-__global__ void __launch_bounds__(kWarpPairThreads, 2) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ MergedShared S[kWarpPairWarps];
-    __shared__ __align__(16) AlphaHot s_list[kWarpPairWarps][kWarpListCap];
-    __shared__ uint2 s_lbc[kWarpPairWarps][kWarpListCap];
-    __shared__ uint64_t s_queue[kWarpPairWarps][kQueue];
+// Compact description of a shared-prime pair for the warp kernel: its two
+// term groups (prime-power table index and exponent of each term), the list
+// sizes, the float/residue form of the group-0 scale 2 fixed(l) fixed(m), and
+// the pair constants.  state: 0 none, 1 fits a warp slice, 2 big, 3 unusable.
+constexpr uint32_t kDescTerms = 10;  // l, m <= 3e7 have at most 5 split primes each
+struct PairDesc {
+    PairCtx ctx;
+    uint32_t base[2][kDescTerms];
+    uint32_t free_count[2];
+    float scale_f;
+    uint32_t scale_res;
+    uint32_t l, m, row;
+    uint8_t count[2];
+    uint8_t e[2][kDescTerms];
+    uint8_t state;
+    uint8_t cc;  // bit 0: the all-central product is a candidate; bit 1: it passes mod 16
+};
+
+__device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, PairDesc& D, uint32_t cap) {
+    MergedShared S;
+    merged_setup(cache, R, q, S, cap);
+    D.l = q.x;
+    D.m = q.y;
+    D.row = q.z;
+    D.state = S.ok == 1 ? 1 : (S.ok == 2 ? 2 : 3);
+    if (S.g[0].count > kDescTerms || S.g[1].count > kDescTerms) D.state = 3;
+    if (D.state != 1) return;
+    for (int g = 0; g < 2; ++g) {
+        D.count[g] = (uint8_t)S.g[g].count;
+        D.free_count[g] = S.g[g].free_count;
+        for (uint32_t t = 0; t < S.g[g].count; ++t) {
+            D.base[g][t] = S.g[g].base[t];
+            D.e[g][t] = (uint8_t)S.g[g].e[t];
+        }
+    }
+    D.scale_f = S.g[0].scale_f;
+    D.scale_res = S.g[0].scale_res;
+    uint32_t cc_c, cc_r;
+    D.ctx = make_ctx(R, q.y, cc_c, cc_r, 0x1p-16f);
+    D.cc = (uint8_t)(cc_c | (cc_r << 1));
+}
+
+// Entry k of side g of a described pair, in float and residues (the decode
+// of group_value, with the block sizes recomputed from the exponents).
+__device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int g, uint32_t k, AlphaHot& out,
+                               uint2& abc) {
+    const uint32_t count = D.count[g];
+    uint32_t suffix[kDescTerms];
+    for (int i = (int)count - 1, acc = 1; i >= 0; --i) {
+        suffix[i] = (uint32_t)acc;
+        acc *= 4 * (int)D.e[g][i] + 1;
+    }
+    float xr = g == 0 ? D.scale_f : 1.f, xi = 0.f;
+    uint32_t rr = g == 0 ? D.scale_res : (1u | (1u << 10) | (1u << 20)), ri = 0u;
+    auto mul = [&](const HotRec& v) {
+        const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
+        uint32_t yr, yi;
+        res_mul(rr, ri, v.rre & 0x7FFFFFFFu, v.rim, yr, yi);
+        xr = nr;
+        xi = ni;
+        rr = yr;
+        ri = yi;
+    };
+    const bool central = k >= D.free_count[g];
+    uint32_t i = 0;
+    if (!central) {
+        while (k >= 2u * D.e[g][i] * suffix[i]) {
+            k -= 2u * D.e[g][i] * suffix[i];
+            ++i;
+        }
+    } else {
+        i = count;
+    }
+    for (uint32_t j = 0; j < i; ++j) mul(cache.pp_hot[D.base[g][j] + 2u * D.e[g][j]]);
+    if (i < count) {
+        const uint32_t r = k / suffix[i];
+        uint32_t rem = k - r * suffix[i];
+        mul(cache.pp_hot[D.base[g][i] + r]);
+        for (uint32_t j = i + 1; j < count; ++j) {
+            const uint32_t below = suffix[j];
+            const uint32_t digit = rem / below;
+            rem -= digit * below;
+            mul(cache.pp_hot[D.base[g][j] + digit]);
+        }
+    }
+    out.re = xr;
+    out.im = xi;
+    out.ra = (rr & 1023u) | (central ? kCentralBit : 0u);
+    out.ia = ri & 1023u;
+    abc = make_uint2(rr, ri);
+}
+
+// Shared-prime pairs, a warp per pair, 32 pairs set up at once: each lane
+// factors one pair's m, splits its terms and computes its pair constants into
+// the warp's descriptor slots; then the warp takes the 32 pairs in turn,
+// builds both lists in its shared slice (float and residue products of the
+// prime-power values) and evaluates all (alpha, beta) combinations in lockstep
+// rounds of 32 with a warp event queue.  Pairs whose lists exceed the slice go
+// to the big-pair queue (one CTA per pair).
+constexpr uint32_t kPairWarps = 4;
+__global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+    __shared__ PairDesc s_desc[kPairWarps][32];
+    __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
+    __shared__ uint2 s_lbc[kPairWarps][kWarpListCap];
+    __shared__ uint64_t s_queue[kPairWarps][kQueue];
     __shared__ uint8_t s_tab[kTableBytes];
-    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kWarpPairThreads) s_tab[i] = buf.tables[i];
+    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kPairWarps * 32) s_tab[i] = buf.tables[i];
     __syncthreads();
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
-    MergedShared& P = S[warp];
+    PairDesc* desc = s_desc[warp];
     AlphaHot* list = s_list[warp];
     uint2* lbc = s_lbc[warp];
     uint64_t* q = s_queue[warp];
     uint32_t qn = 0;
     const uint32_t count = min(*buf.merged_count, buf.merged_cap);
-    const uint32_t stride = gridDim.x * kWarpPairWarps;
-    for (uint32_t qi = blockIdx.x * kWarpPairWarps + warp; qi < count; qi += stride) {
-        __syncwarp();
-        const uint4 e = buf.merged_queue[qi];
-        const RowInfo& R = buf.row_info[e.z];
-        if (lane == 0) {
-            merged_setup(cache, R, e, P, kWarpListCap);
-            if (P.ok == 1) {
-                uint32_t cc_c, cc_r;
-                P.ctx = make_ctx(R, e.y, cc_c, cc_r);
-                P.cc_cand = cc_c;
-                P.cc_r16 = cc_r;
-            } else if (P.ok == 2) {
+    const uint32_t stride = gridDim.x * kPairWarps * 32;
+    for (uint32_t b0 = (blockIdx.x * kPairWarps + warp) * 32; b0 < count; b0 += stride) {
+        const uint32_t qi = b0 + lane;
+        if (qi < count) {
+            const uint4 e = buf.merged_queue[qi];
+            pair_desc_setup(cache, buf.row_info[e.z], e, desc[lane], kWarpListCap);
+            if (desc[lane].state == 2) {
                 unsigned int idx = atomicAdd(buf.big_count, 1u);
                 if (idx < buf.big_cap)
                     buf.big_queue[idx] = e;
                 else
                     atomicOr(buf.error_flags, 2u);
-            } else {
+            } else if (desc[lane].state == 3) {
                 atomicOr(buf.error_flags, 2u);
             }
-        }
-        __syncwarp();
-        if (P.ok != 1) continue;
-        const uint32_t na = P.g[0].free_count + 1, nb = P.g[1].free_count + 1;
-        for (uint32_t k = lane; k < na + nb; k += 32) {
-            const int side = k < na ? 0 : 1;
-            const uint32_t idx = side ? k - na : k;
-            i128 re, im;
-            group_value(cache, P.g[side], idx, re, im);
-            list_entry(re, im, idx == P.g[side].free_count, list[k], lbc[k]);
+        } else {
+            desc[lane].state = 0;
         }
         __syncwarp();
         Acc acc{0, 0, 0, 0, 0, 0};
-        if (lane == 0) {
-            acc.prod += 1;
-            acc.cand += P.cc_cand;
-            acc.r16 += P.cc_r16;
-        }
-        const PairCtx c = P.ctx;
-        const uint32_t total = na * nb;
-        const float rcp = 1.0f / (float)nb;
-        auto handle = [&](uint64_t ev) {
-            const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
-            add_event(acc, merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c, ka, kb,
-                                        (uint32_t)P.l, P.row, s_tab, (uint32_t)cache.limit, &buf));
-        };
-        for (uint32_t base = 0; base < total; base += 32) {
-            const uint32_t k = base + lane;
-            uint32_t flags = 0, ka = 0;
-            int32_t kb = 0;
-            if (k < total) {
-                ka = (uint32_t)((float)k * rcp);
-                kb = (int32_t)k - (int32_t)(ka * nb);
-                while (kb < 0) {
-                    --ka;
-                    kb += (int32_t)nb;
-                }
-                while (kb >= (int32_t)nb) {
-                    ++ka;
-                    kb -= (int32_t)nb;
-                }
-                const AlphaHot a = list[ka], bh = list[na + kb];
-                flags = pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c,
-                                                       s_tab, acc)
-                                     : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
-                                                        c, s_tab, acc);
+        uint32_t cur_row = 0xFFFFFFFFu;
+        for (uint32_t i = 0; i < 32; ++i) {
+            const PairDesc& D = desc[i];
+            if (D.state != 1) continue;
+            if (D.row != cur_row) {
+                if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
+                cur_row = D.row;
             }
-            if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags))) drain(q, qn, 32, handle);
+            if (lane == 0) {
+                acc.prod += 1;
+                acc.cand += D.cc & 1u;
+                acc.r16 += (D.cc >> 1) & 1u;
+            }
+            const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1;
+            for (uint32_t k = lane; k < na + nb; k += 32) {
+                const int side = k < na ? 0 : 1;
+                desc_value_hot(cache, D, side, side ? k - na : k, list[k], lbc[k]);
+            }
+            __syncwarp();
+            const PairCtx c = D.ctx;
+            const uint32_t l = D.l, row = D.row;
+            const uint32_t total = na * nb;
+            const float rcp = 1.0f / (float)nb;
+            auto handle = [&](uint64_t ev) {
+                const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+                add_event(acc, merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c,
+                                            ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf));
+            };
+            const bool dual = pair_dual(c);
+            for (uint32_t base = 0; base < total; base += 32) {
+                const uint32_t k = base + lane;
+                uint32_t flags = 0, ka = 0;
+                int32_t kb = 0;
+                if (k < total) {
+                    ka = (uint32_t)((float)k * rcp);
+                    kb = (int32_t)k - (int32_t)(ka * nb);
+                    while (kb < 0) {
+                        --ka;
+                        kb += (int32_t)nb;
+                    }
+                    while (kb >= (int32_t)nb) {
+                        ++ka;
+                        kb -= (int32_t)nb;
+                    }
+                    const AlphaHot a = list[ka], bh = list[na + kb];
+                    flags = dual ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
+                                                   c, s_tab, acc)
+                                 : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
+                                                    c, s_tab, acc);
+                }
+                if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags))) drain(q, qn, 32, handle);
+            }
+            while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
+            __syncwarp();
         }
-        while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
-        flush_acc(acc, &buf.rows[P.row], true);
+        if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
+        __syncwarp();
     }
 }
 
@@ -1113,7 +1285,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         if (threadIdx.x == 0) {
             merged_setup(cache, R, e, S, kMergedListCap);
             uint32_t cc_c, cc_r;
-            S.ctx = make_ctx(R, e.y, cc_c, cc_r);
+            S.ctx = make_ctx(R, e.y, cc_c, cc_r, 0x1p-16f);
             S.cc_cand = cc_c;
             S.cc_r16 = cc_r;
             if (S.ok != 1) atomicOr(buf.error_flags, 2u);
@@ -1124,9 +1296,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         for (uint32_t k = threadIdx.x; k < na + nb; k += kMergedThreads) {
             const int side = k < na ? 0 : 1;
             const uint32_t idx = side ? k - na : k;
-            i128 re, im;
-            group_value(cache, S.g[side], idx, re, im);
-            list_entry(re, im, idx == S.g[side].free_count, s_list[k], s_lbc[k]);
+            group_value_hot(cache, S.g[side], idx, s_list[k], s_lbc[k]);
         }
         __syncthreads();
         Acc acc{0, 0, 0, 0, 0, 0};
@@ -1345,7 +1515,7 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf, int ctas,
                           cudaStream_t stream) {
     (void)count;
-    merged_kernel<<<ctas, kWarpPairThreads, 0, stream>>>(cache, buf);
+    merged_kernel<<<ctas, kPairWarps * 32, 0, stream>>>(cache, buf);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     merged_big_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
