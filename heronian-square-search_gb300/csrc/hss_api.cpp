@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "hss_api_status.h"
+#include "hss_ctx.h"
 #include "hss_kernels.h"
 #include "hss_prep.h"
 
@@ -40,71 +41,8 @@ constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
 constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
 
-struct Request;
 
 }  // namespace
-
-struct hss_ctx {
-    int device = 0;
-    uint64_t limit = 0;
-    hss_opts opts{};
-    int sm_count = 0;
-    std::string err;
-
-    // host mirrors used to build work items
-    std::vector<uint32_t> seg_off;
-    std::vector<uint32_t> spf;
-    uint64_t records = 0, ref_flattened = 0, ref_cached = 0;
-    double prep_seconds = 0;
-
-    DeviceCache dev{};
-    std::vector<void*> allocations;
-
-    // launch buffers
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    RowCounts* d_rows = nullptr;
-    size_t rows_cap = 0;
-    DevHit* d_hits = nullptr;
-    uint32_t hit_cap = 0;
-    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count [5] exact_count
-    uint4* d_big = nullptr;          // shared-prime pairs too big for a warp
-    uint32_t big_cap = 0;
-    ExactItem* d_exact = nullptr;    // exact work queue
-    uint32_t exact_cap = 0;
-    uint4* d_merged = nullptr;
-    uint32_t merged_cap = 0;
-    uint8_t* d_tables = nullptr;
-    WorkItem* d_items = nullptr;
-    size_t items_cap = 0;
-    WorkItem* h_items = nullptr;  // pinned
-    size_t h_items_cap = 0;
-    RowCounts* h_rows = nullptr;  // pinned
-    size_t h_rows_cap = 0;
-    RowInfo* d_row_info = nullptr;  // constants of the call's rows
-    RowInfo* h_row_info = nullptr;  // pinned
-    size_t row_info_cap = 0;
-
-    std::mutex gpu_mu;  // serialises device work on the handle
-
-    // per-call accounting: event triples (before main kernel, after it,
-    // after the shared-prime kernels) for every launch group
-    std::vector<cudaEvent_t> event_pool;
-    size_t events_used = 0;
-    std::vector<std::array<cudaEvent_t, 3>> marks;
-    uint32_t launches = 0;
-    uint64_t h2d_bytes = 0, d2h_bytes = 0;
-
-    // serving
-    std::mutex serve_mu;
-    std::condition_variable serve_cv;
-    std::thread serve_thread;
-    bool serving = false, serve_stop = false;
-    uint32_t max_active = 0, wave_items = 0;
-    uint64_t next_id = 1;
-    std::map<uint64_t, Request*> requests;
-    std::deque<uint64_t> pending;
-};
 
 namespace {
 
@@ -833,7 +771,7 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
 
 // ------------------------------------------------------------------ serving
 
-namespace {
+namespace hss {
 
 struct Request {
     uint64_t id = 0, first = 0, last = 0;

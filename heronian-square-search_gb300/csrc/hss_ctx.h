@@ -1,0 +1,82 @@
+// hss_ctx.h - the handle behind hss_t, shared by the host sources.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "hss_api_status.h"
+#include "hss_kernels.h"
+
+namespace hss {
+struct Request;
+}
+
+struct hss_ctx {
+    int device = 0;
+    uint64_t limit = 0;
+    hss_opts opts{};
+    int sm_count = 0;
+    std::string err;
+
+    // host mirrors used to build work items
+    std::vector<uint32_t> seg_off;
+    std::vector<uint32_t> spf;
+    uint64_t records = 0, ref_flattened = 0, ref_cached = 0;
+    double prep_seconds = 0;
+
+    hss::DeviceCache dev{};
+    std::vector<void*> allocations;
+
+    // launch buffers
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    hss::RowCounts* d_rows = nullptr;
+    size_t rows_cap = 0;
+    hss::DevHit* d_hits = nullptr;
+    uint32_t hit_cap = 0;
+    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count [5] exact_count
+    uint4* d_big = nullptr;          // shared-prime pairs too big for a warp
+    uint32_t big_cap = 0;
+    hss::ExactItem* d_exact = nullptr;    // exact work queue
+    uint32_t exact_cap = 0;
+    uint4* d_merged = nullptr;
+    uint32_t merged_cap = 0;
+    uint8_t* d_tables = nullptr;
+    hss::WorkItem* d_items = nullptr;
+    size_t items_cap = 0;
+    hss::WorkItem* h_items = nullptr;  // pinned
+    size_t h_items_cap = 0;
+    hss::RowCounts* h_rows = nullptr;  // pinned
+    size_t h_rows_cap = 0;
+    hss::RowInfo* d_row_info = nullptr;  // constants of the call's rows
+    hss::RowInfo* h_row_info = nullptr;  // pinned
+    size_t row_info_cap = 0;
+
+    std::mutex gpu_mu;  // serialises device work on the handle
+
+    // per-call accounting: event triples (before main kernel, after it,
+    // after the shared-prime kernels) for every launch group
+    std::vector<cudaEvent_t> event_pool;
+    size_t events_used = 0;
+    std::vector<std::array<cudaEvent_t, 3>> marks;
+    uint32_t launches = 0;
+    uint64_t h2d_bytes = 0, d2h_bytes = 0;
+
+    // serving
+    std::mutex serve_mu;
+    std::condition_variable serve_cv;
+    std::thread serve_thread;
+    bool serving = false, serve_stop = false;
+    uint32_t max_active = 0, wave_items = 0;
+    uint64_t next_id = 1;
+    std::map<uint64_t, hss::Request*> requests;
+    std::deque<uint64_t> pending;
+};
+

@@ -1,0 +1,247 @@
+// hss_noalloc.cu - a search entry point that allocates no memory.
+//
+// hss_search grows its per-call buffers (row table, work items, counters,
+// the shared-prime and exact-work queues, pinned staging) with cudaMalloc and
+// cudaMallocHost when a call needs more than the last one.  Some callers
+// cannot allow that at search time: processes whose device memory is owned by
+// a pool or an embedding runtime fixed at start-up, or loops that cannot take
+// the implicit synchronisation an allocation brings.  hss_search_noalloc runs
+// the same batched launch sequence (persistent kernel, shared-prime kernels,
+// exact kernel) with all per-call device scratch in one file-scope array of
+// kNoAllocBytes that is part of the library image, and host staging in static
+// buffers.  Every GPU that loads the library holds the array until the process
+// exits.
+//
+// Set-up: the array's name is a host-side stand-in, not a device address.
+// The first call on a device, with that device current, looks the address up
+// with cudaGetSymbolAddress and keeps it; that first call should come before
+// any stream capture.  Calls share the array and keep the last call's
+// contents; everything that must start at zero (counters, queue cursors) is
+// cleared by each call.  Calls are serialised within the process; calls that
+// overlap on the GPU race on the array.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "hss_ctx.h"
+#include "hss_kernels.h"
+#include "hss_prep.h"
+
+namespace {
+
+using namespace hss;
+
+// Limits of one call, and the layout of the scratch array.
+constexpr uint32_t kNaRows = 64;          // root rows per call
+constexpr uint32_t kNaItems = 8192;       // work items per call
+constexpr uint32_t kNaMerged = 1u << 20;  // pairs sharing a split prime per call
+constexpr uint32_t kNaBig = 1u << 14;     // of which too big for one warp
+constexpr uint32_t kNaExact = 1u << 16;   // exact work items per call
+constexpr uint32_t kNaHits = 4096;        // hits kept per call (as the reference, gpu_search_v42.cu:177-178)
+constexpr uint32_t kNaCtrl = 8;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+constexpr size_t kOffCtrl = 0;
+constexpr size_t kOffRows = align256(kOffCtrl + kNaCtrl * sizeof(unsigned int));
+constexpr size_t kOffRowInfo = align256(kOffRows + kNaRows * sizeof(RowCounts));
+constexpr size_t kOffHits = align256(kOffRowInfo + kNaRows * sizeof(RowInfo));
+constexpr size_t kOffItems = align256(kOffHits + kNaHits * sizeof(DevHit));
+constexpr size_t kOffMerged = align256(kOffItems + kNaItems * sizeof(WorkItem));
+constexpr size_t kOffBig = align256(kOffMerged + (size_t)kNaMerged * sizeof(uint4));
+constexpr size_t kOffExact = align256(kOffBig + kNaBig * sizeof(uint4));
+constexpr size_t kNoAllocBytes = align256(kOffExact + kNaExact * sizeof(ExactItem));
+static_assert(kNoAllocBytes <= (24u << 20), "scratch stays within 24 MiB");
+
+static __device__ __align__(256) unsigned char g_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+unsigned char* g_scratch_ptr[kMaxDevices];  // device address of g_scratch, per device
+std::mutex g_mu;                            // serialises calls (shared host and device scratch)
+
+// Host staging (static, so the call allocates nothing).
+RowInfo g_host_rows[kNaRows];
+WorkItem g_host_items[kNaItems];
+RowCounts g_host_counts[kNaRows];
+DevHit g_host_hits[kNaHits];
+unsigned int g_host_ctrl[kNaCtrl];
+
+// Failures are reported by status code only (recording a message would
+// allocate): HSS_ERR_LIMIT - the interval needs more than the scratch holds;
+// HSS_ERR_OVERFLOW - a queue filled up; HSS_ERR_CUDA / HSS_ERR_NO_DEVICE.
+int fail(hss_t* h, int status, const char* msg) {
+    (void)h;
+    (void)msg;
+    return status;
+}
+
+// Address of the scratch array on the current device (looked up once).
+int scratch_on(hss_t* h, unsigned char** out) {
+    if (h->device < 0 || h->device >= kMaxDevices) return fail(h, HSS_ERR_NO_DEVICE, "device index beyond table");
+    if (!g_scratch_ptr[h->device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess) return fail(h, HSS_ERR_CUDA, cudaGetErrorString(e));
+        g_scratch_ptr[h->device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_ptr[h->device];
+    return HSS_OK;
+}
+
+// Pairs of row l that can share a split prime with some m in [l, N].
+uint64_t shared_bound(const hss_t* h, uint64_t l) {
+    NumberFactors f = factor_number(h->spf.data(), l);
+    uint64_t n = h->limit, total = 0;
+    for (uint32_t mask = 1; mask < (1u << f.count); ++mask) {
+        uint64_t prod = 1;
+        int bits = 0;
+        bool over = false;
+        for (uint32_t i = 0; i < f.count; ++i)
+            if (mask & (1u << i)) {
+                prod *= f.primes[i];
+                ++bits;
+                if (prod > n) over = true;
+            }
+        if (over) continue;
+        uint64_t cnt = n / prod - (l - 1) / prod;
+        total = (bits & 1) ? total + cnt : total - cnt;
+    }
+    return total;
+}
+
+#define NA_CUDA(call)                                                \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return fail(h, HSS_ERR_CUDA, cudaGetErrorString(e_)); \
+    } while (0)
+
+int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits, uint32_t hit_cap,
+        uint32_t* nhits) {
+    const uint32_t rows = (uint32_t)(last - first + 1);
+    if (rows > kNaRows) return fail(h, HSS_ERR_LIMIT, "hss_search_noalloc: more than 64 root rows");
+    uint64_t shared = 0;
+    uint32_t alpha_cap = 1;
+    for (uint32_t r = 0; r < rows; ++r) {
+        shared += shared_bound(h, first + r);
+        alpha_cap = std::max(alpha_cap, h->seg_off[first + r + 1] - h->seg_off[first + r]);
+    }
+    if (shared > kNaMerged)
+        return fail(h, HSS_ERR_LIMIT, "hss_search_noalloc: more pairs sharing a split prime than the scratch holds");
+    NA_CUDA(cudaSetDevice(h->device));
+    unsigned char* base = nullptr;
+    if (int s = scratch_on(h, &base)) return s;
+
+    // row constants and work items (each row cut into equal m-ranges)
+    const uint32_t per_row = kNaItems / rows;
+    uint32_t n_items = 0;
+    for (uint32_t r = 0; r < rows; ++r) {
+        const uint64_t l = first + r;
+        fill_row_info(h->spf.data(), h->seg_off.data(), h->limit, l, &g_host_rows[r]);
+        const uint64_t span = h->limit - l + 1;
+        const uint64_t pieces = std::min<uint64_t>(per_row, (span + 31) / 32);
+        const uint64_t tile = (span + pieces - 1) / pieces;
+        for (uint64_t m = l; m <= h->limit; m += tile)
+            g_host_items[n_items++] =
+                WorkItem{(uint32_t)l, (uint32_t)m, (uint32_t)std::min<uint64_t>(m + tile, h->limit + 1), r};
+    }
+
+    LaunchBuffers b;
+    unsigned int* ctrl = reinterpret_cast<unsigned int*>(base + kOffCtrl);
+    b.rows = reinterpret_cast<RowCounts*>(base + kOffRows);
+    b.hits = reinterpret_cast<DevHit*>(base + kOffHits);
+    b.hit_count = ctrl + 0;
+    b.hit_cap = kNaHits;
+    b.merged_queue = reinterpret_cast<uint4*>(base + kOffMerged);
+    b.merged_count = ctrl + 1;
+    b.merged_cap = kNaMerged;
+    b.next_item = ctrl + 2;
+    b.error_flags = ctrl + 3;
+    b.big_queue = reinterpret_cast<uint4*>(base + kOffBig);
+    b.big_count = ctrl + 4;
+    b.big_cap = kNaBig;
+    b.exact_queue = reinterpret_cast<ExactItem*>(base + kOffExact);
+    b.exact_count = ctrl + 5;
+    b.exact_cap = kNaExact;
+    b.tables = h->d_tables;
+    b.row_info = reinterpret_cast<const RowInfo*>(base + kOffRowInfo);
+
+    cudaStream_t st = h->stream;
+    NA_CUDA(cudaMemsetAsync(base + kOffCtrl, 0, kNaCtrl * sizeof(unsigned int), st));
+    NA_CUDA(cudaMemsetAsync(base + kOffRows, 0, rows * sizeof(RowCounts), st));
+    NA_CUDA(cudaMemcpyAsync(base + kOffRowInfo, g_host_rows, rows * sizeof(RowInfo), cudaMemcpyHostToDevice, st));
+    NA_CUDA(cudaMemcpyAsync(base + kOffItems, g_host_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice, st));
+    BatchedConfig cfg;
+    cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
+    cfg.min_blocks =
+        h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 6 : cfg.threads == 512 ? 1 : 3);
+    cfg.alpha_cap = alpha_cap;
+    cfg.ctas = h->sm_count * batched_max_ctas_per_sm(cfg.threads, cfg.min_blocks,
+                                                     batched_smem_bytes(cfg.threads, alpha_cap));
+    NA_CUDA(cudaEventRecord(h->ev0, st));
+    NA_CUDA(launch_batched(h->dev, reinterpret_cast<const WorkItem*>(base + kOffItems), n_items, cfg, b, st));
+    NA_CUDA(launch_merged(h->dev, 0, b, h->sm_count * 4, st));
+    NA_CUDA(launch_exact(h->dev, b, h->sm_count * 4, st));
+    NA_CUDA(cudaEventRecord(h->ev1, st));
+    NA_CUDA(cudaMemcpyAsync(g_host_ctrl, ctrl, sizeof g_host_ctrl, cudaMemcpyDeviceToHost, st));
+    NA_CUDA(cudaMemcpyAsync(g_host_counts, b.rows, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost, st));
+    NA_CUDA(cudaStreamSynchronize(st));
+    if (g_host_ctrl[3]) return fail(h, HSS_ERR_OVERFLOW, "hss_search_noalloc: a scratch queue overflowed");
+    const uint32_t nh = std::min(g_host_ctrl[0], kNaHits);
+    if (nh) NA_CUDA(cudaMemcpy(g_host_hits, b.hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
+    float ms = 0;
+    NA_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+
+    std::sort(g_host_hits, g_host_hits + nh, [](const DevHit& x, const DevHit& y) {
+        if (x.l != y.l) return x.l < y.l;
+        if (x.m != y.m) return x.m < y.m;
+        return x.n < y.n;
+    });
+    const uint32_t unique = (uint32_t)(std::unique(g_host_hits, g_host_hits + nh,
+                                                   [](const DevHit& x, const DevHit& y) {
+                                                       return x.l == y.l && x.m == y.m && x.n == y.n;
+                                                   }) -
+                                       g_host_hits);
+    memset(out, 0, sizeof *out);
+    for (uint32_t r = 0; r < rows; ++r) {
+        const RowCounts& c = g_host_counts[r];
+        out->pairs += h->limit - (first + r) + 1;
+        out->processed += c.processed;
+        out->products += c.products;
+        out->candidates += c.candidates;
+        out->r16 += c.r16;
+        out->exact += c.exact;
+        out->merged += c.merged;
+        out->merged_products += c.mproducts;
+        out->merged_candidates += c.mcandidates;
+        out->merged_r16 += c.mr16;
+    }
+    const uint32_t found = g_host_ctrl[0] > kNaHits ? g_host_ctrl[0] : unique;
+    out->hits = found;
+    out->kernel_ms = ms;
+    out->launches = 4;
+    out->h2d_bytes = rows * sizeof(RowInfo) + n_items * sizeof(WorkItem);
+    out->d2h_bytes = sizeof g_host_ctrl + rows * sizeof(RowCounts) + nh * sizeof(DevHit);
+    for (uint32_t i = 0; i < unique && i < hit_cap && hits; ++i) {
+        hits[i].l = g_host_hits[i].l;
+        hits[i].m = g_host_hits[i].m;
+        hits[i].n = g_host_hits[i].n;
+        hits[i].area4_lo = g_host_hits[i].area4_lo;
+        hits[i].area4_hi = g_host_hits[i].area4_hi;
+        hits[i].heron_ok = g_host_hits[i].heron_ok;
+        hits[i].reserved = 0;
+    }
+    if (nhits) *nhits = found;
+    return HSS_OK;
+}
+
+}  // namespace
+
+extern "C" int hss_search_noalloc(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
+                                  uint32_t hit_cap, uint32_t* nhits) {
+    if (!h || !out) return HSS_ERR_ARGUMENT;
+    if (first < 1 || first > last || last > h->limit) return HSS_ERR_ARGUMENT;
+    std::lock_guard<std::mutex> process_lock(g_mu);
+    std::lock_guard<std::mutex> handle_lock(h->gpu_mu);
+    return run(h, first, last, out, hits, hit_cap, nhits);
+}

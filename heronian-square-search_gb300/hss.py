@@ -94,6 +94,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
                                       p(ctypes.c_int64), u32, p(u32)]
     lib.hss_search.argtypes = [ctypes.c_void_p, u64, u64, i32, p(HssCounts), p(u64), p(HssHit), u32,
                                p(u32)]
+    lib.hss_search_noalloc.argtypes = [ctypes.c_void_p, u64, u64, p(HssCounts), p(HssHit), u32, p(u32)]
     lib.hss_search_many.argtypes = [ctypes.c_void_p, p(u64), p(u64), u32, p(HssCounts),
                                     p(HssCounts), p(HssHit), u32, p(u32)]
     lib.hss_autotune.argtypes = [ctypes.c_void_p, u64, u64, p(HssOpts), p(HssTuneTrial), u32, p(u32)]
@@ -180,6 +181,19 @@ class Search:
         self._check(st)
         h, ok = _hits(hits, min(nh.value, hit_cap))
         return SearchResult(counts.as_dict(), h, ok, list(row_buf) if rows else None)
+
+    def search_noalloc(self, first: int, last: int, hit_cap: int = 64) -> SearchResult:
+        """hss_search_noalloc: the batched search with static scratch (at most
+        64 rows per call); raises HssError on its limits."""
+        counts = HssCounts()
+        hits = (HssHit * hit_cap)()
+        nh = ctypes.c_uint32()
+        st = self.lib.hss_search_noalloc(self.handle, first, last, ctypes.byref(counts), hits, hit_cap,
+                                         ctypes.byref(nh))
+        if st:
+            raise HssError(st, self.lib.hss_strerror(st).decode())
+        h, ok = _hits(hits, min(nh.value, hit_cap))
+        return SearchResult(counts.as_dict(), h, ok)
 
     def search_many(self, intervals: Sequence[Tuple[int, int]], hit_cap: int = 4096):
         n = len(intervals)

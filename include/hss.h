@@ -159,6 +159,25 @@ typedef struct {
 int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tune_trial* trials,
                  uint32_t max_trials, uint32_t* ntrials);
 
+/* The same search as hss_search (batched path), for callers that cannot
+ * allocate memory while searching - processes whose device memory is owned
+ * by a pool or an embedding runtime fixed at start-up, or loops that cannot
+ * take the synchronisation an allocation implies.  hss_search grows its
+ * per-call buffers with cudaMalloc / cudaMallocHost; this call allocates
+ * nothing: its device scratch is one array of about 19 MiB that is static in
+ * the library (every GPU that loads the library holds it until the process
+ * exits), its host staging is static too, and the handle's cache, stream and
+ * tables (made by hss_open) are the inputs.  Limits per call: at most 64 root
+ * rows and at most 2^20 pairs sharing a split prime (HSS_ERR_LIMIT beyond
+ * them); up to 4096 hits kept.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and should come before any
+ * stream capture.  Calls share the array: they are serialised within the
+ * process, clear what must start at zero, and calls that overlap on the GPU
+ * race.  Errors are reported by status only (hss_last_error is not updated).
+ * No counterpart in the reference. */
+int hss_search_noalloc(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
+                       uint32_t hit_cap, uint32_t* nhits);
+
 /* Batched search of several intervals in one persistent launch sequence:
  * intervals i = [firsts[i], lasts[i]].  per_interval (count entries) receives
  * each interval's counters; hits of all intervals are returned together. */
