@@ -35,8 +35,8 @@ namespace {
 
 constexpr uint32_t kDefaultHitCap = 4096;      // gpu_search_v42.cu:177-178
 constexpr uint32_t kPlainBatch = 512;          // gpu_search_v42.cu:457
-constexpr uint32_t kDefaultItemTarget = 1u << 20;
-constexpr uint32_t kTileCap = 8192;            // largest m-range of one item
+constexpr uint32_t kDefaultItemTarget = 1u << 22;
+constexpr uint32_t kTileCap = 16384;           // largest m-range of one item
 constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
 constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
@@ -212,7 +212,7 @@ struct RowRef {
 // about item_target alpha*beta evaluations (at most kTileCap roots), then
 // ordered by m so that concurrently running items read the same m-side
 // records from L2.  Returns the largest row segment and m-range.
-size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap) {
+size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap, uint32_t min_tile) {
     const uint64_t n = h->limit;
     const uint32_t target = h->opts.item_target ? h->opts.item_target : kDefaultItemTarget;
     std::vector<uint32_t> tile(nrows);
@@ -225,7 +225,7 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
         double per_m = (double)(h->seg_off[n + 1] - h->seg_off[l]) / (double)(n - l + 1);
         double t = (double)target / ((double)na * std::max(per_m, 1.0));
         uint32_t tm = t >= kTileCap ? kTileCap : (uint32_t)t;
-        tm = std::max(kTileMin, tm & ~(kTileMin - 1));
+        tm = std::max(min_tile, tm & ~(kTileMin - 1));
         tile[r] = tm;
         total += (n - l + 1 + tm - 1) / tm;
     }
@@ -286,7 +286,9 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     // the pinned item buffer may still be read by the previous group's copy
     HSS_CUDA(h, cudaStreamSynchronize(h->stream));
     uint32_t acap = 1;
-    size_t n_items = build_items(h, rows, nrows, &acap);
+    const int threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
+    // every warp of a CTA claims 128 roots at a time: items span at least that
+    size_t n_items = build_items(h, rows, nrows, &acap, (uint32_t)threads / 32 * 128);
     if (n_items == (size_t)-1) return HSS_ERR_MEMORY;
     if (n_items == 0) return HSS_OK;
     HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
@@ -296,7 +298,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
-    cfg.min_blocks = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 6 : cfg.threads == 512 ? 1 : 3);
+    cfg.min_blocks = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 4 : cfg.threads == 512 ? 1 : 2);
     cfg.alpha_cap = acap;
     size_t smem = batched_smem_bytes(cfg.threads, acap);
     int per_sm = batched_max_ctas_per_sm(cfg.threads, cfg.min_blocks, smem);
@@ -671,7 +673,7 @@ int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tu
                  uint32_t max_trials, uint32_t* ntrials) {
     if (!h) return HSS_ERR_ARGUMENT;
     static const uint32_t kVariants[][2] = {{128, 4}, {128, 6}, {256, 2}, {256, 3}, {512, 1}};
-    static const uint32_t kTargets[] = {1u << 19, 1u << 20, 1u << 21};
+    static const uint32_t kTargets[] = {1u << 21, 1u << 22, 1u << 23};
     const hss_opts saved = h->opts;
     hss_opts chosen = saved;
     float best_ms = 0;

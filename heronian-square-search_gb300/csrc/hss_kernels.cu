@@ -493,8 +493,9 @@ __device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t ki
 
 // Event handler of the cached path: record j against the row value whose
 // exact value is at index ka; counts come back by value (x: candidates, y:
-// mod-16 survivors).
-__device__ __forceinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
+// mod-16 survivors).  Out of line, so that the hot loops stay small in the
+// instruction cache; it has no 128-bit code, so the call costs few registers.
+__device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
                                               uint32_t j, uint32_t l, uint32_t row, const uint8_t* tab,
                                               uint32_t limit, const LaunchBuffers* buf) {
     Acc acc{0, 0, 0, 0, 0, 0};
@@ -678,32 +679,43 @@ struct BatchedShared {
     uint32_t next_m;
 };
 
-__device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t owner, uint32_t k, uint32_t flags) {
-    return (uint64_t)j | ((uint64_t)owner << 32) | ((uint64_t)k << 37) | ((uint64_t)flags << 50);
+constexpr uint32_t kRootsPerLane = 4;  // a warp claims 128 roots at a time
+
+__device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t slot, uint32_t k, uint32_t flags) {
+    return (uint64_t)j | ((uint64_t)slot << 32) | ((uint64_t)k << 40) | ((uint64_t)flags << 53);
 }
 
+// One pass over the records of the warp's 128 roots (the dual or the
+// non-dual ones): lane i holds roots slot = 32u + i (u < 4) with cnt[u]
+// records starting at s0[u].  Record r of the pass (lane-major order, so
+// consecutive records are consecutive in memory) is found by a binary search
+// over the lanes' inclusive prefix sums, then within the owner lane.
 template <bool DUAL>
 __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint2* s_abc, uint32_t na,
-                                             const PairCtx* wctx, uint32_t cnt, uint32_t s0, uint32_t lane,
+                                             const PairCtx* wctx, const uint32_t (&cnt)[kRootsPerLane],
+                                             const uint32_t (&s0)[kRootsPerLane], uint32_t lane,
                                              const DeviceCache& cache, const uint8_t* s_tab, uint32_t a0, uint64_t l,
                                              uint32_t row, const LaunchBuffers& buf, uint64_t* q, uint32_t& qn,
                                              Acc& acc) {
-    uint32_t incl = cnt;
+    uint32_t mine = 0;
+#pragma unroll
+    for (uint32_t u = 0; u < kRootsPerLane; ++u) mine += cnt[u];
+    uint32_t incl = mine;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
         uint32_t t = __shfl_up_sync(kFull, incl, d);
         if (lane >= (uint32_t)d) incl += t;
     }
     const uint32_t total = __shfl_sync(kFull, incl, 31);
-    const uint32_t excl = incl - cnt;
+    if (total == 0) return;
+    const uint32_t excl = incl - mine;
     auto handle = [&](uint64_t ev) {
-        const uint32_t j = (uint32_t)ev, owner = (uint32_t)(ev >> 32) & 31u, k = (uint32_t)(ev >> 37) & 0x1FFFu;
-        add_event(acc, cached_event((uint32_t)(ev >> 50), s_alpha[k], s_abc[k], cache.hot[j], wctx[owner], a0 + k, j,
+        const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
+        add_event(acc, cached_event((uint32_t)(ev >> 53), s_alpha[k], s_abc[k], cache.hot[j], wctx[slot], a0 + k, j,
                                     (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf));
     };
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t r = base + lane;
-        // owner = first lane whose inclusive prefix exceeds r
         uint32_t owner = 0;
 #pragma unroll
         for (uint32_t step = 16; step >= 1; step >>= 1) {
@@ -711,9 +723,21 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
             if (v <= r) owner += step;
         }
         owner &= 31u;
-        const uint32_t j = __shfl_sync(kFull, s0, owner) + r - __shfl_sync(kFull, excl, owner);
+        uint32_t off = r - __shfl_sync(kFull, excl, owner);
+        uint32_t slot = owner, j = 0;
+#pragma unroll
+        for (uint32_t u = 0; u < kRootsPerLane; ++u) {
+            const uint32_t cu = __shfl_sync(kFull, cnt[u], owner);
+            const uint32_t su = __shfl_sync(kFull, s0[u], owner);
+            if (off < cu && slot == owner) {
+                slot = 32 * u + owner + 1024u;  // mark found
+                j = su + off;
+            }
+            if (slot == owner) off -= cu;
+        }
+        slot = (slot - 1024u) & 127u;
         const bool live = r < total;
-        const PairCtx c = wctx[owner];
+        const PairCtx c = wctx[slot];
         const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
         const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
         const bool cb = (b.rre & kCentralBit) != 0;
@@ -721,7 +745,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
             if (live) flags = eval_fast<DUAL>(a, b.re, b.im, bra, bia, cb, c, s_tab, acc);
-            if (queue_push(q, qn, flags != 0, batched_event_word(j, owner, k, flags))) drain(q, qn, 32, handle);
+            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, handle);
         }
     }
     while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
@@ -732,17 +756,18 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
                                                            uint32_t n_items, uint32_t alpha_cap,
                                                            const LaunchBuffers buf) {
     constexpr uint32_t kWarps = NT / 32;
+    constexpr uint32_t kChunk = 32 * kRootsPerLane;
     extern __shared__ __align__(16) unsigned char smem[];
     AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
     uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
     PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_abc + alpha_cap);
-    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * 32);
+    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * kChunk);
     uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_queue + kWarps * kQueue);
     __shared__ BatchedShared S;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid / 32;
     uint64_t* q = s_queue + warp * kQueue;
-    PairCtx* wctx = s_wctx + warp * 32;
+    PairCtx* wctx = s_wctx + warp * kChunk;
     uint32_t qn = 0;
     for (uint32_t i = tid; i < kTableBytes; i += NT) s_tab[i] = buf.tables[i];
     Acc acc{0, 0, 0, 0, 0, 0};
@@ -763,22 +788,29 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
         const uint32_t nm = w.m1 - w.m0;
         for (;;) {
             uint32_t c0 = 0;
-            if (lane == 0) c0 = atomicAdd(&S.next_m, 32u);
+            if (lane == 0) c0 = atomicAdd(&S.next_m, kChunk);
             c0 = __shfl_sync(kFull, c0, 0);
             if (c0 >= nm) break;
-            const uint32_t m = w.m0 + c0 + lane;
-            uint32_t kind = kSkip, s0 = 0, cnt = 0;
-            bool dual = false;
-            if (c0 + lane < nm) {
-                s0 = cache.seg_off[m];
-                const uint32_t s1 = cache.seg_off[m + 1];
-                kind = classify(R, m, s1 - s0 - 1);
+            uint32_t cnt_single[kRootsPerLane], cnt_dual[kRootsPerLane], s0[kRootsPerLane];
+            bool any_dual = false;
+#pragma unroll
+            for (uint32_t u = 0; u < kRootsPerLane; ++u) {
+                cnt_single[u] = cnt_dual[u] = s0[u] = 0;
+                if (c0 + 32 * u + lane >= nm) continue;
+                const uint32_t m = w.m0 + c0 + 32 * u + lane;
+                const uint32_t seg0 = cache.seg_off[m], seg1 = cache.seg_off[m + 1];
+                const uint32_t kind = classify(R, m, seg1 - seg0 - 1);
                 if (kind == kCached) {
                     uint32_t cc_c, cc_r;
                     const PairCtx c = make_ctx(R, m, cc_c, cc_r);
-                    wctx[lane] = c;
-                    dual = pair_dual(c);
-                    cnt = s1 - s0;
+                    wctx[32 * u + lane] = c;
+                    s0[u] = seg0;
+                    if (pair_dual(c)) {
+                        cnt_dual[u] = seg1 - seg0;
+                        any_dual = true;
+                    } else {
+                        cnt_single[u] = seg1 - seg0;
+                    }
                     acc.processed += 1;
                     acc.prod += 1;
                     acc.cand += cc_c;
@@ -790,11 +822,11 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
                 }
             }
             __syncwarp();
-            batched_pass<false>(s_alpha, s_abc, na, wctx, dual ? 0u : cnt, s0, lane, cache, s_tab, a0, w.l, w.row,
-                                buf, q, qn, acc);
-            if (__any_sync(kFull, dual))
-                batched_pass<true>(s_alpha, s_abc, na, wctx, dual ? cnt : 0u, s0, lane, cache, s_tab, a0, w.l, w.row,
-                                   buf, q, qn, acc);
+            batched_pass<false>(s_alpha, s_abc, na, wctx, cnt_single, s0, lane, cache, s_tab, a0, w.l, w.row, buf,
+                                q, qn, acc);
+            if (__any_sync(kFull, any_dual))
+                batched_pass<true>(s_alpha, s_abc, na, wctx, cnt_dual, s0, lane, cache, s_tab, a0, w.l, w.row, buf, q,
+                                   qn, acc);
             __syncwarp();
         }
         flush_acc(acc, &buf.rows[w.row]);
@@ -993,7 +1025,7 @@ __device__ void list_entry(i128 re, i128 im, bool central, AlphaHot& a, uint2& a
 }
 
 // One event of a shared-prime pair: list entries ka (alpha side) and kb.
-__device__ __forceinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc, AlphaHot bh, uint2 bbc,
+__device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc, AlphaHot bh, uint2 bbc,
                                               PairCtx c, uint32_t ka, uint32_t kb, uint32_t l, uint32_t row,
                                               const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf) {
     Acc acc{0, 0, 0, 0, 0, 0};
@@ -1471,8 +1503,9 @@ void build_residue_tables(uint8_t* out) {
 
 size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
     const uint32_t warps = (uint32_t)threads / 32;
-    return (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) + (size_t)warps * 32 * sizeof(PairCtx) +
-           (size_t)warps * kQueue * sizeof(uint64_t) + kTableBytes;
+    return (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) +
+           (size_t)warps * 32 * kRootsPerLane * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
+           kTableBytes;
 }
 
 // Compiled (threads, min CTAs per SM) variants of the persistent kernel; the

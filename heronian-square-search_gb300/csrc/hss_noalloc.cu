@@ -174,7 +174,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
     cfg.min_blocks =
-        h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 6 : cfg.threads == 512 ? 1 : 3);
+        h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 4 : cfg.threads == 512 ? 1 : 2);
     cfg.alpha_cap = alpha_cap;
     cfg.ctas = h->sm_count * batched_max_ctas_per_sm(cfg.threads, cfg.min_blocks,
                                                      batched_smem_bytes(cfg.threads, alpha_cap));
