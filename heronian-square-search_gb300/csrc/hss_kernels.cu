@@ -13,13 +13,13 @@
 //
 // How it is computed here.  The reference multiplies every product out in
 // 128-bit arithmetic.  These kernels decide almost every product from
-//   * residues of the product's coordinates mod 720, 625 and 1547, formed from
+//   * residues of the product's coordinates mod 9360, 625 and 119, formed from
 //     per-value residues with 32-bit multiplies (exact), and
 //   * float coordinates with a proven error bound: |z| = 2 l^2 m^2 is known per
 //     pair, so every coordinate's float error is below eps = 2 l^2 m^2 2^-20,
 // and only go to exact 128-bit arithmetic when a decision is within eps of a
 // window boundary, or when z passes every residue filter and a fourth root n
-// inside z's float bounds matches z modulo 720 * 625 * 1547 (a possible hit).
+// inside z's float bounds matches z modulo 9360 * 625 * 119 (a possible hit).
 // Counts are therefore exact and every hit is confirmed exactly and rechecked
 // in 256-bit arithmetic.
 //
@@ -50,7 +50,7 @@ using i128 = __int128;
 constexpr uint32_t kSqA = kModA * kModA;
 constexpr uint32_t kSqB = kModB * kModB;
 constexpr uint32_t kSqC = kModC * kModC;
-constexpr uint32_t kTabA = 0, kTabB = 720, kTabC = 720 + 625;
+constexpr uint32_t kTabA = 0, kTabB = kModA, kTabC = kModA + kModB;
 constexpr uint32_t kSlices = 8;            // plain kernel: blocks per row
 constexpr uint32_t kPlainThreads = 128;    // plain kernel: threads per block
 constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
@@ -68,13 +68,13 @@ struct PairCtx {
     float hi2, hi2o;             // z = S + t counted iff t <= hi2; maybe iff t <= hi2o
     float eps;                   // bound on |float - exact| of a product coordinate
     float sf;                    // S = l^4 + m^4 as float
-    uint32_t sres;               // S mod 720 | mod 625 << 10 | mod 1547 << 20 | flag5 << 31
+    uint32_t sres;               // S mod kModA | mod kModB << 14 | mod kModC << 24 | flag5 << 31
     uint32_t dinv;               // inverse of D mod 2^32 (0: pair not on this path)
     uint32_t dthr;               // floor((2^32 - 1) / (8 D))
     uint32_t m;
 };
 
-// Row-side value in shared memory: coordinates as float and their mod-720
+// Row-side value in shared memory: coordinates as float and their mod-kModA
 // residues (bit 31 of ra: central value); B/C residues kept alongside.
 struct AlphaHot {
     float re, im;
@@ -87,7 +87,7 @@ struct Acc {
 
 // Event flags per product p (bits 4p .. 4p+3).
 constexpr uint32_t kEvU = 1;   // undecided: count the whole product exactly
-constexpr uint32_t kEvDx = 2;  // orientation (x, y) counted, z passed mod 720: deep + root filters
+constexpr uint32_t kEvDx = 2;  // orientation (x, y) counted, z passed mod kModA: deep + root filters
 constexpr uint32_t kEvDy = 4;  // the same for orientation (y, x)
 constexpr uint32_t kEvB = 8;   // non-dual pair with both orientations gated: (y, x) still to do
 
@@ -316,7 +316,7 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
     const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
     const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
     const float f1 = a.re * br, f2 = a.im * bi, f3 = a.re * bi, f4 = a.im * br;
-    const uint32_t sA = c.sres & 1023u;
+    const uint32_t sA = c.sres & kMaskA;
     const uint32_t sel = (c.sres >> 31) ? 4u : 2u;
     uint32_t flags = 0, cnt = 0, r16 = 0;
 #pragma unroll
@@ -362,33 +362,59 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
 }
 
 // A possible hit needs some n in [m, N] with n^4 = z.  From z's float bounds
-// (|error| below sf 2^-22 + eps + |z| 2^-22) take the n with n^4 inside them
-// (plus a margin for the float fourth root: n < 2^25, so a relative 2^-20
-// and 2 units cover it) and keep the candidate only if some such n has
-// n^4 = z mod 720, 625 and 1547.  Float and 32-bit integer arithmetic only.
-__device__ bool root_filter(float zf, const PairCtx& c, uint32_t zA, uint32_t zB, uint32_t zC, uint32_t n_limit) {
+// (|error| below sf 2^-22 + eps + |z| 2^-22) take the window of n with n^4
+// inside them, and keep the candidate only if some n of the window has
+// n^4 = z mod 9360, 625 and 119.  The float fourth root sqrtf(sqrtf(x)) is
+// within 1.5 * 2^-24 relative of x^(1/4) (two correctly rounded square
+// roots), so scaling by 1 -+ 2^-22 (and rounding once more) keeps the bounds
+// on the safe side; 2 units are added on top.  Float and 32-bit integers only.
+__device__ __forceinline__ void root_window(float zf, const PairCtx& c, uint32_t n_limit, uint32_t& nlo,
+                                            uint32_t& nhi) {
     const float ez = c.sf * 0x1p-22f + c.eps + fabsf(zf) * 0x1p-22f;
     const float lo = fmaxf(zf - ez, 0.f), hi = zf + ez;
-    const float rlo = sqrtf(sqrtf(lo)) * (1.f - 0x1p-20f), rhi = sqrtf(sqrtf(hi)) * (1.f + 0x1p-20f);
+    const float rlo = sqrtf(sqrtf(lo)) * (1.f - 0x1p-22f), rhi = sqrtf(sqrtf(hi)) * (1.f + 0x1p-22f);
     const uint32_t m = c.m & 0x7FFFFFFFu;
     const uint32_t flo = __float2uint_rd(rlo), fhi = __float2uint_ru(rhi);
-    const uint32_t nlo = flo > m + 2 ? flo - 2 : m;
-    const uint32_t nhi = fhi + 2 < n_limit ? fhi + 2 : n_limit;
-    for (uint32_t n = nlo; n <= nhi; ++n) {
-        if (pow4_mod(n % kModA, kModA) != zA) continue;
-        if (pow4_mod(n % kModB, kModB) != zB) continue;
-        if (pow4_mod(n % kModC, kModC) != zC) continue;
-        return true;
+    nlo = flo > m + 2 ? flo - 2 : m;
+    nhi = fhi + 2 < n_limit ? fhi + 2 : n_limit;
+}
+
+__device__ __forceinline__ bool root_match(uint32_t n, uint32_t zres) {
+    return pow4_mod(n % kModA, kModA) == (zres & kMaskA) &&
+           pow4_mod(n % kModB, kModB) == ((zres >> kShiftB) & kMaskB) &&
+           pow4_mod(n % kModC, kModC) == ((zres >> kShiftC) & kMaskC);
+}
+
+// One thread scans the window (paths without a warp queue).
+__device__ bool root_scan(uint32_t nlo, uint32_t nhi, uint32_t zres) {
+    for (uint32_t n = nlo; n <= nhi; ++n)
+        if (root_match(n, zres)) return true;
+    return false;
+}
+
+// A root-filter request left by an event for its warp: the window and packed
+// residues of one counted term, and the orientation (tag = 2p + o) whose
+// exact hit test it gates.  The warp scans each request together, one n per
+// lane, instead of one lane walking the window while the others wait.
+struct RootReq {
+    uint32_t nlo, nhi, zres, tag;
+};
+constexpr uint32_t kReqPerLane = 2;  // per event; further terms are scanned by the lane itself
+
+__device__ __forceinline__ bool root_scan_warp(const RootReq& rq, uint32_t lane) {
+    for (uint32_t base = rq.nlo; base <= rq.nhi; base += 32) {
+        const uint32_t n = base + lane;
+        if (__any_sync(kFull, n <= rq.nhi && root_match(n, rq.zres))) return true;
     }
     return false;
 }
 
-// Residues of the product's coordinates modulo 625 (field 1) or 1547
+// Residues of the product's coordinates modulo 625 (field 1) or 119
 // (field 2) from the packed value residues.
 __device__ __forceinline__ void coord_res(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw, int field,
                                           int p, uint32_t& x, uint32_t& y) {
-    const uint32_t shift = field == 1 ? 10u : 20u;
-    const uint32_t mask = field == 1 ? 1023u : 2047u;
+    const uint32_t shift = field == 1 ? kShiftB : kShiftC;
+    const uint32_t mask = field == 1 ? kMaskB : kMaskC;
     const uint32_t M = field == 1 ? kModB : kModC;
     const uint32_t sq = field == 1 ? kSqB : kSqC;
     uint32_t ar = (arw >> shift) & mask, ai = (aiw >> shift) & mask, br = (brw >> shift) & mask,
@@ -413,18 +439,24 @@ constexpr uint32_t kExCount = 0, kExOrient = 1, kExHit = 2;
 // Work of one event (one lane), in float and 32-bit integer arithmetic only:
 // an undecided product is queued for exact counting; the (y, x) orientation
 // of a non-dual product whose both orientations passed is decided and
-// counted; every counted orientation whose z passed mod 720 goes through the
-// mod-625 / mod-1547 filters and the fourth-root filter, and survivors are
+// counted; every counted orientation whose z passed mod 9360 goes through the
+// mod-625 / mod-119 filters and the fourth-root filter, and survivors are
 // queued for the exact hit test.  push(kind | p << 2 | o << 3) queues work.
+//
+// With `slots` (warp-queue paths) the root filter of up to kReqPerLane terms
+// is left to the warp as requests (*nreq of them); orientations that the lane
+// itself found possible are returned in *passed (bit 2p + o) instead of being
+// queued, so that the caller queues each orientation once.
 template <class PushFn>
 __device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a, uint32_t arw, uint32_t aiw,
                                               const HotRec& b, const PairCtx& c, uint32_t n_limit,
-                                              const uint8_t* tab, Acc& acc, PushFn push) {
+                                              const uint8_t* tab, Acc& acc, PushFn push, RootReq* slots = nullptr,
+                                              uint32_t* nreq = nullptr, uint32_t* passed = nullptr) {
     const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
-    const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+    const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
     const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
     const float f1 = a.re * b.re, f2 = a.im * b.im, f3 = a.re * b.im, f4 = a.im * b.re;
-    const uint32_t sA = c.sres & 1023u, sB = (c.sres >> 10) & 1023u, sC = (c.sres >> 20) & 2047u;
+    const uint32_t sA = c.sres & kMaskA, sB = (c.sres >> kShiftB) & kMaskB, sC = (c.sres >> kShiftC) & kMaskC;
     const bool flag5 = (c.sres >> 31) != 0;
     const uint32_t sel = flag5 ? 4u : 2u;
     for (int p = 0; p < 2; ++p) {
@@ -473,9 +505,20 @@ __device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a,
                 if (flag5 ? zB != 0 : !tab[kTabB + zB]) continue;
                 if (!tab[kTabC + zC]) continue;
                 const float zf = term ? c.sf + t : c.sf - t;
-                if (root_filter(zf, c, term ? zA2 : zA1, zB, zC, n_limit)) hit_possible = true;
+                uint32_t nlo, nhi;
+                root_window(zf, c, n_limit, nlo, nhi);
+                const uint32_t zres = (term ? zA2 : zA1) | (zB << kShiftB) | (zC << kShiftC);
+                if (slots && *nreq < kReqPerLane)
+                    slots[(*nreq)++] = RootReq{nlo, nhi, zres, 2u * (uint32_t)p + (uint32_t)o};
+                else if (root_scan(nlo, nhi, zres))
+                    hit_possible = true;
             }
-            if (hit_possible) push(kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
+            if (hit_possible) {
+                if (slots)
+                    *passed |= 1u << (2 * p + o);
+                else
+                    push(kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
+            }
         }
     }
 }
@@ -495,13 +538,24 @@ __device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t ki
 // exact value is at index ka; counts come back by value (x: candidates, y:
 // mod-16 survivors).  Out of line, so that the hot loops stay small in the
 // instruction cache; it has no 128-bit code, so the call costs few registers.
+// With `slots`, x also carries the root requests left (bits 16-19) and the
+// orientations already found possible (bits 20-23).
 __device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
                                               uint32_t j, uint32_t l, uint32_t row, const uint8_t* tab,
-                                              uint32_t limit, const LaunchBuffers* buf) {
+                                              uint32_t limit, const LaunchBuffers* buf, RootReq* slots = nullptr) {
     Acc acc{0, 0, 0, 0, 0, 0};
+    uint32_t nreq = 0, passed = 0;
     process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
-                  [&](uint32_t kind) { push_exact(*buf, kind, ka, j, l, pair_m(c), row, false); });
-    return make_uint2(acc.cand, acc.r16);
+                  [&](uint32_t kind) { push_exact(*buf, kind, ka, j, l, pair_m(c), row, false); }, slots, &nreq,
+                  &passed);
+    return make_uint2(acc.cand | (nreq << 16) | (passed << 20), acc.r16);
+}
+
+// Queues the exact hit test of each orientation in `tags` (bit 2p + o).
+__device__ __noinline__ void push_hits(const LaunchBuffers* buf, uint32_t tags, uint32_t a, uint32_t b, uint32_t l,
+                                       uint32_t m, uint32_t row, bool shared_prime) {
+    for (uint32_t t = 0; t < 4; ++t)
+        if ((tags >> t) & 1u) push_exact(*buf, kExHit | (t >> 1) << 2 | (t & 1u) << 3, a, b, l, m, row, shared_prime);
 }
 
 __device__ __forceinline__ void add_event(Acc& acc, uint2 r) {
@@ -576,7 +630,7 @@ __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uin
     uint32_t sA = (R.lmodA + pow4_mod(mA, kModA)) % kModA;
     uint32_t sB = (R.lmodB + pow4_mod(mB, kModB)) % kModB;
     uint32_t sC = (R.lmodC + pow4_mod(mC, kModC)) % kModC;
-    c.sres = sA | (sB << 10) | (sC << 20) | (f5 ? 0x80000000u : 0u);
+    c.sres = sA | (sB << kShiftB) | (sC << kShiftC) | (f5 ? 0x80000000u : 0u);
     uint32_t areaA = 2u * (R.l2modA * (uint32_t)(m2 % kModA) % kModA);
     bool cc = area_gate(areaA, c.dinv, c.dthr) && w <= 0;
     cc_cand = cc ? 1u : 0u;
@@ -593,14 +647,14 @@ __device__ __forceinline__ void scale2(const HotRec& h, AlphaHot& a, uint2& abc)
     uint32_t out[2];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-        uint32_t ra = w[i] & 1023u, rb = (w[i] >> 10) & 1023u, rc = (w[i] >> 20) & 2047u;
+        uint32_t ra = w[i] & kMaskA, rb = (w[i] >> kShiftB) & kMaskB, rc = (w[i] >> kShiftC) & kMaskC;
         ra = 2 * ra >= kModA ? 2 * ra - kModA : 2 * ra;
         rb = 2 * rb >= kModB ? 2 * rb - kModB : 2 * rb;
         rc = 2 * rc >= kModC ? 2 * rc - kModC : 2 * rc;
-        out[i] = ra | (rb << 10) | (rc << 20);
+        out[i] = ra | (rb << kShiftB) | (rc << kShiftC);
     }
-    a.ra = (out[0] & 1023u) | (h.rre & kCentralBit);
-    a.ia = out[1] & 1023u;
+    a.ra = (out[0] & kMaskA) | (h.rre & kCentralBit);
+    a.ia = out[1] & kMaskA;
     abc = make_uint2(out[0], out[1]);
 }
 
@@ -650,12 +704,36 @@ __device__ __forceinline__ bool queue_push(uint64_t* q, uint32_t& count, bool ha
 }
 
 // Processes the first `n` events of a warp queue, one per lane, then moves
-// the rest to the front.  All 32 lanes must call it.
-template <class Handler>
-__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, Handler handle) {
+// the rest to the front.  handle(ev, slots) returns the event's root requests
+// left in `slots` (bits 0-3) and the orientations it found possible itself
+// (bits 4-7); the warp then scans every request together, and hit(ev, tags)
+// queues the exact hit test of each possible orientation of the lane's event.
+// All 32 lanes must call it.
+template <class Handler, class HitFn>
+__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, RootReq* wreq, Handler handle,
+                                      HitFn hit) {
     __syncwarp();
     const uint32_t lane = threadIdx.x & 31;
-    if (lane < n) handle(q[lane]);
+    uint64_t ev = 0;
+    uint32_t info = 0;
+    if (lane < n) {
+        ev = q[lane];
+        info = handle(ev, wreq + lane * kReqPerLane);
+    }
+    __syncwarp();
+    const uint32_t nreq = info & 15u;
+    uint32_t passed = (info >> 4) & 15u;
+    uint32_t todo = __ballot_sync(kFull, nreq != 0);
+    while (todo) {
+        const uint32_t src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t cnt = __shfl_sync(kFull, nreq, src);
+        for (uint32_t r = 0; r < cnt; ++r) {
+            const RootReq rq = wreq[src * kReqPerLane + r];
+            if (root_scan_warp(rq, lane) && lane == src) passed |= 1u << rq.tag;
+        }
+    }
+    if (passed) hit(ev, passed);
     __syncwarp();
     const uint32_t rest = count - n;
     if (lane < rest) q[lane] = q[n + lane];
@@ -696,7 +774,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
                                              const uint32_t (&s0)[kRootsPerLane], uint32_t lane,
                                              const DeviceCache& cache, const uint8_t* s_tab, uint32_t a0, uint64_t l,
                                              uint32_t row, const LaunchBuffers& buf, uint64_t* q, uint32_t& qn,
-                                             Acc& acc) {
+                                             RootReq* wreq, Acc& acc) {
     uint32_t mine = 0;
 #pragma unroll
     for (uint32_t u = 0; u < kRootsPerLane; ++u) mine += cnt[u];
@@ -709,10 +787,17 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
     const uint32_t total = __shfl_sync(kFull, incl, 31);
     if (total == 0) return;
     const uint32_t excl = incl - mine;
-    auto handle = [&](uint64_t ev) {
+    auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
-        add_event(acc, cached_event((uint32_t)(ev >> 53), s_alpha[k], s_abc[k], cache.hot[j], wctx[slot], a0 + k, j,
-                                    (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf));
+        const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], s_abc[k], cache.hot[j], wctx[slot], a0 + k, j,
+                                     (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
+        acc.cand += r.x & 0xFFFFu;
+        acc.r16 += r.y;
+        return r.x >> 16;
+    };
+    auto hit = [&](uint64_t ev, uint32_t tags) {
+        const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
+        push_hits(&buf, tags, a0 + k, j, (uint32_t)l, pair_m(wctx[slot]), row, false);
     };
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t r = base + lane;
@@ -739,16 +824,16 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
         const bool live = r < total;
         const PairCtx c = wctx[slot];
         const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
-        const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+        const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
         const bool cb = (b.rre & kCentralBit) != 0;
         for (uint32_t k = 0; k < na; ++k) {
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
             if (live) flags = eval_fast<DUAL>(a, b.re, b.im, bra, bia, cb, c, s_tab, acc);
-            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, handle);
+            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, handle, hit);
         }
     }
-    while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
+    while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, handle, hit);
 }
 
 template <int NT, int MINB>
@@ -762,12 +847,14 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
     uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
     PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_abc + alpha_cap);
     uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * kChunk);
-    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_queue + kWarps * kQueue);
+    RootReq* s_req = reinterpret_cast<RootReq*>(s_queue + kWarps * kQueue);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kWarps * 32 * kReqPerLane);
     __shared__ BatchedShared S;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid / 32;
     uint64_t* q = s_queue + warp * kQueue;
     PairCtx* wctx = s_wctx + warp * kChunk;
+    RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
     for (uint32_t i = tid; i < kTableBytes; i += NT) s_tab[i] = buf.tables[i];
     Acc acc{0, 0, 0, 0, 0, 0};
@@ -823,10 +910,10 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
             }
             __syncwarp();
             batched_pass<false>(s_alpha, s_abc, na, wctx, cnt_single, s0, lane, cache, s_tab, a0, w.l, w.row, buf,
-                                q, qn, acc);
+                                q, qn, wreq, acc);
             if (__any_sync(kFull, any_dual))
                 batched_pass<true>(s_alpha, s_abc, na, wctx, cnt_dual, s0, lane, cache, s_tab, a0, w.l, w.row, buf, q,
-                                   qn, acc);
+                                   qn, wreq, acc);
             __syncwarp();
         }
         flush_acc(acc, &buf.rows[w.row]);
@@ -869,7 +956,7 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
         acc.r16 += cc_r;
         for (uint32_t j = s0; j < s1; ++j) {
             const HotRec b = cache.hot[j];
-            const uint32_t bra = b.rre & 1023u, bia = b.rim & 1023u;
+            const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
             const bool cb = (b.rre & kCentralBit) != 0;
             for (uint32_t k = 0; k < na; ++k) {
                 const uint32_t flags = pair_dual(c) ? eval_fast<true>(s_alpha[k], b.re, b.im, bra, bia, cb, c, s_tab, acc)
@@ -953,14 +1040,14 @@ __device__ void group_value(const DeviceCache& cache, const Group& g, uint32_t k
     im = xi;
 }
 
-// Complex product of packed residues (mod 720 | 625 << 10 | 1547 << 20).
+// Complex product of packed residues (mod 9360 | 625 << 14 | 119 << 24).
 __device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, uint32_t bi, uint32_t& xr,
                                         uint32_t& xi) {
     uint32_t outr = 0, outi = 0;
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-        const uint32_t shift = f == 0 ? 0u : (f == 1 ? 10u : 20u);
-        const uint32_t mask = f == 2 ? 2047u : 1023u;
+        const uint32_t shift = f == 0 ? 0u : (f == 1 ? kShiftB : kShiftC);
+        const uint32_t mask = f == 0 ? kMaskA : (f == 1 ? kMaskB : kMaskC);
         const uint32_t M = f == 0 ? kModA : (f == 1 ? kModB : kModC);
         const uint32_t a0 = (ar >> shift) & mask, a1 = (ai >> shift) & mask;
         const uint32_t b0 = (br >> shift) & mask, b1 = (bi >> shift) & mask;
@@ -1010,8 +1097,8 @@ __device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32
     }
     out.re = xr;
     out.im = xi;
-    out.ra = (rr & 1023u) | (central ? kCentralBit : 0u);
-    out.ia = ri & 1023u;
+    out.ra = (rr & kMaskA) | (central ? kCentralBit : 0u);
+    out.ia = ri & kMaskA;
     abc = make_uint2(rr, ri);
 }
 
@@ -1019,20 +1106,23 @@ __device__ void list_entry(i128 re, i128 im, bool central, AlphaHot& a, uint2& a
     uint32_t rw = pack_residues(re), iw = pack_residues(im);
     a.re = i128_to_float(re);
     a.im = i128_to_float(im);
-    a.ra = (rw & 1023u) | (central ? kCentralBit : 0u);
-    a.ia = iw & 1023u;
+    a.ra = (rw & kMaskA) | (central ? kCentralBit : 0u);
+    a.ia = iw & kMaskA;
     abc = make_uint2(rw, iw);
 }
 
 // One event of a shared-prime pair: list entries ka (alpha side) and kb.
 __device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc, AlphaHot bh, uint2 bbc,
                                               PairCtx c, uint32_t ka, uint32_t kb, uint32_t l, uint32_t row,
-                                              const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf) {
+                                              const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf,
+                                              RootReq* slots = nullptr) {
     Acc acc{0, 0, 0, 0, 0, 0};
+    uint32_t nreq = 0, passed = 0;
     const HotRec b{bh.re, bh.im, bbc.x | (bh.ra & kCentralBit), bbc.y};
     process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
-                  [&](uint32_t kind) { push_exact(*buf, kind, ka, kb, l, pair_m(c), row, true); });
-    return make_uint2(acc.cand, acc.r16);
+                  [&](uint32_t kind) { push_exact(*buf, kind, ka, kb, l, pair_m(c), row, true); }, slots, &nreq,
+                  &passed);
+    return make_uint2(acc.cand | (nreq << 16) | (passed << 20), acc.r16);
 }
 
 // Splits the merged terms of (l, m) into two groups (largest terms first,
@@ -1102,7 +1192,7 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
     S.g[0].scale_f = i128_to_float(fixed);
     S.g[0].scale_res = pack_residues(fixed);
     S.g[1].scale_f = 1.f;
-    S.g[1].scale_res = 1u | (1u << 10) | (1u << 20);
+    S.g[1].scale_res = kResOne;
     if (S.ok == 1 && S.g[0].free_count + S.g[1].free_count + 2 > list_cap) S.ok = 2;
 }
 
@@ -1159,7 +1249,7 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
         acc *= 4 * (int)D.e[g][i] + 1;
     }
     float xr = g == 0 ? D.scale_f : 1.f, xi = 0.f;
-    uint32_t rr = g == 0 ? D.scale_res : (1u | (1u << 10) | (1u << 20)), ri = 0u;
+    uint32_t rr = g == 0 ? D.scale_res : kResOne, ri = 0u;
     auto mul = [&](const HotRec& v) {
         const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
         uint32_t yr, yi;
@@ -1193,8 +1283,8 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
     }
     out.re = xr;
     out.im = xi;
-    out.ra = (rr & 1023u) | (central ? kCentralBit : 0u);
-    out.ia = ri & 1023u;
+    out.ra = (rr & kMaskA) | (central ? kCentralBit : 0u);
+    out.ia = ri & kMaskA;
     abc = make_uint2(rr, ri);
 }
 
@@ -1211,7 +1301,10 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
     __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
     __shared__ uint2 s_lbc[kPairWarps][kWarpListCap];
     __shared__ uint64_t s_queue[kPairWarps][kQueue];
-    __shared__ uint8_t s_tab[kTableBytes];
+    // dynamic (static use is near 48 KB): root requests, then the tables
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    RootReq* s_req = reinterpret_cast<RootReq*>(s_dyn);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kPairWarps * 32 * kReqPerLane);
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kPairWarps * 32) s_tab[i] = buf.tables[i];
     __syncthreads();
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
@@ -1219,6 +1312,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
     AlphaHot* list = s_list[warp];
     uint2* lbc = s_lbc[warp];
     uint64_t* q = s_queue[warp];
+    RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
     const uint32_t count = min(*buf.merged_count, buf.merged_cap);
     const uint32_t stride = gridDim.x * kPairWarps * 32;
@@ -1264,10 +1358,17 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             const uint32_t l = D.l, row = D.row;
             const uint32_t total = na * nb;
             const float rcp = 1.0f / (float)nb;
-            auto handle = [&](uint64_t ev) {
+            auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
-                add_event(acc, merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c,
-                                            ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf));
+                const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c,
+                                             ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
+                acc.cand += r.x & 0xFFFFu;
+                acc.r16 += r.y;
+                return r.x >> 16;
+            };
+            auto hit = [&](uint64_t ev, uint32_t tags) {
+                const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+                push_hits(&buf, tags, ka, kb, l, pair_m(c), row, true);
             };
             const bool dual = pair_dual(c);
             for (uint32_t base = 0; base < total; base += 32) {
@@ -1291,9 +1392,10 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                                  : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
                                                     c, s_tab, acc);
                 }
-                if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags))) drain(q, qn, 32, handle);
+                if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags)))
+                    drain(q, qn, 32, wreq, handle, hit);
             }
-            while (qn) drain(q, qn, qn < 32 ? qn : 32, handle);
+            while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, handle, hit);
             __syncwarp();
         }
         if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
@@ -1489,23 +1591,22 @@ void build_residue_tables(uint8_t* out) {
             if (x * x % m * x % m * x % m == r) return true;
         return false;
     };
-    for (uint32_t z = 0; z < 720; ++z) {
+    for (uint32_t z = 0; z < kModA; ++z) {
         bool m16 = (z & 15u) <= 1u;
-        bool m9 = is4(z % 9, 9);
+        bool m9 = is4(z % 9, 9) && is4(z % 13, 13);
         bool m5 = is4(z % 5, 5);
         out[kTabA + z] = (uint8_t)((m16 ? 1u : 0u) | ((m16 && m9 && m5) ? 2u : 0u) |
                                    ((m16 && m9 && z % 5 == 0) ? 4u : 0u));
     }
-    for (uint32_t z = 0; z < 625; ++z) out[kTabB + z] = is4(z, 625) ? 1 : 0;
-    for (uint32_t z = 0; z < 1547; ++z)
-        out[kTabC + z] = (is4(z % 7, 7) && is4(z % 13, 13) && is4(z % 17, 17)) ? 1 : 0;
+    for (uint32_t z = 0; z < kModB; ++z) out[kTabB + z] = is4(z, kModB) ? 1 : 0;
+    for (uint32_t z = 0; z < kModC; ++z) out[kTabC + z] = (is4(z % 7, 7) && is4(z % 17, 17)) ? 1 : 0;
 }
 
 size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
     const uint32_t warps = (uint32_t)threads / 32;
     return (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) +
            (size_t)warps * 32 * kRootsPerLane * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
-           kTableBytes;
+           (size_t)warps * 32 * kReqPerLane * sizeof(RootReq) + kTableBytes;
 }
 
 // Compiled (threads, min CTAs per SM) variants of the persistent kernel; the
@@ -1548,8 +1649,12 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf, int ctas,
                           cudaStream_t stream) {
     (void)count;
-    merged_kernel<<<ctas, kPairWarps * 32, 0, stream>>>(cache, buf);
-    cudaError_t e = cudaGetLastError();
+    const size_t smem = kPairWarps * 32 * kReqPerLane * sizeof(RootReq) + kTableBytes;
+    cudaError_t e = cudaFuncSetAttribute((const void*)merged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     merged_big_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
     return cudaGetLastError();

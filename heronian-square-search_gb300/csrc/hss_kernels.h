@@ -8,11 +8,13 @@
 namespace hss {
 
 // Sizes of the residue tables the kernels stage in shared memory:
-// tab720[z mod 720] bit0: z mod 16 in {0,1}; bit1: bit0 and z mod 9 and
-// z mod 5 fourth-power residues; bit2: bit0, z mod 9 residue and 5 | z.
-// tab625[z mod 625]: fourth-power residue mod 625.  tab1547[z mod 1547]:
-// fourth-power residue mod 7, 13 and 17 (gpu_search_v42.cu:166-170).
-constexpr uint32_t kTableBytes = 720 + 625 + 1547;
+// tabA[z mod 9360] bit0: z mod 16 in {0,1}; bit1: bit0 and z mod 9, 5 and 13
+// fourth-power residues; bit2: bit0, z mod 9 and 13 residues and 5 | z.
+// tabB[z mod 625]: fourth-power residue mod 625.  tabC[z mod 119]:
+// fourth-power residue mod 7 and 17.  Together they hold the conditions of
+// the reference's mod 16, 9, 5, 625 and 7*13*17 tables
+// (gpu_search_v42.cu:166-170), regrouped by modulus.
+constexpr uint32_t kTableBytes = kModA + kModB + kModC;
 void build_residue_tables(uint8_t* out /* kTableBytes */);
 
 // Constants of one root row, built on the host for every row of a launch
@@ -23,7 +25,7 @@ struct RowInfo {
     uint64_t l, l2;
     unsigned __int128 l4, n4;
     uint64_t fixed;             // prod of non-split p^(2a) of l
-    uint32_t lmodA, lmodB, lmodC, l2modA;  // l^4 mod 720, 625, 1547; l^2 mod 720
+    uint32_t lmodA, lmodB, lmodC, l2modA;  // l^4 mod kModA, kModB, kModC; l^2 mod kModA
     uint32_t l3, l5, leven, nodd;          // 3 | l, 5 | l, l even, number of odd primes
     uint32_t pinv[9], pthr[9];
     uint32_t psplit;            // bit i set when odd prime i is = 1 mod 4

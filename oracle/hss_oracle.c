@@ -334,8 +334,10 @@ typedef struct {
     uint64_t products, candidates, r16, processed;
 } ora_row_counts_t;
 
-/* All m in [l, N] for one root l (search_v18.cpp:329-371). */
-static void process_row(ora_ctx_t *c, uint64_t l, ora_row_counts_t *out) {
+/* All m in [l, N] for one root l (search_v18.cpp:329-371); with step > 1
+ * only m = m0, m0 + step, ... (a bounded sample of the row for timing). */
+static void process_row_stride(ora_ctx_t *c, uint64_t l, uint64_t m0, uint64_t step,
+                               ora_row_counts_t *out) {
     const ora_tables_t *t = c->t;
     const uint64_t n = t->limit;
     const ora_number_t *a = &t->info[l];
@@ -344,7 +346,7 @@ static void process_row(ora_ctx_t *c, uint64_t l, ora_row_counts_t *out) {
     c->n4 = (u128)n * n * n * n;
     c->products = c->candidates = c->r16 = 0;
     uint64_t processed = 0;
-    for (uint64_t m = l; m <= n; ++m) {
+    for (uint64_t m = m0; m <= n; m += step) {
         if ((l & 1) == 0 && (m & 1) == 0) continue;
         const ora_number_t *b = &t->info[m];
         if (a->inert_part > 1 && gcd_u64(a->inert_part, m) > 1) continue;
@@ -379,6 +381,10 @@ static void process_row(ora_ctx_t *c, uint64_t l, ora_row_counts_t *out) {
     out->candidates = c->candidates;
     out->r16 = c->r16;
     out->processed = processed;
+}
+
+static void process_row(ora_ctx_t *c, uint64_t l, ora_row_counts_t *out) {
+    process_row_stride(c, l, l, 1, out);
 }
 
 /* ------------------------------------------------------------ public API */
@@ -489,6 +495,62 @@ int hss_oracle_search(void *tables, uint64_t first, uint64_t last, int threads,
     free(job.hits);
     free(job.rows);
     pthread_mutex_destroy(&job.lock);
+    return 0;
+}
+
+/* Strided sample of rows, for timing the CPU search on a bounded share of a
+ * batch: job j searches root ls[j] over m = m0s[j], m0s[j] + step, ... <= N,
+ * one job per thread at a time.  Per job, *logical receives the number of m
+ * visited (the logical pairs) and *candidates the candidates counted.
+ * Returns 0, or -1 on invalid arguments. */
+typedef struct {
+    const ora_tables_t *t;
+    const uint64_t *ls, *m0s;
+    uint64_t step;
+    uint32_t njobs;
+    _Atomic uint32_t next;
+    uint64_t *logical, *candidates;
+} ora_sample_t;
+
+static void *sample_worker(void *arg) {
+    ora_sample_t *s = arg;
+    ora_ctx_t c;
+    memset(&c, 0, sizeof c);
+    c.t = s->t;
+    for (;;) {
+        uint32_t j = atomic_fetch_add(&s->next, 1);
+        if (j >= s->njobs) break;
+        ora_row_counts_t out;
+        process_row_stride(&c, s->ls[j], s->m0s[j], s->step, &out);
+        if (s->logical) s->logical[j] = (s->t->limit - s->m0s[j]) / s->step + 1;
+        if (s->candidates) s->candidates[j] = out.candidates;
+    }
+    free(c.hits);
+    return NULL;
+}
+
+int hss_oracle_sample(void *tables, const uint64_t *ls, const uint64_t *m0s, uint64_t step,
+                      uint32_t njobs, int threads, uint64_t *logical, uint64_t *candidates) {
+    ora_tables_t *t = tables;
+    if (!t || !ls || !m0s || step == 0 || njobs == 0) return -1;
+    for (uint32_t j = 0; j < njobs; ++j)
+        if (ls[j] == 0 || m0s[j] < ls[j] || m0s[j] > t->limit) return -1;
+    if (threads < 1) threads = 1;
+    if ((uint32_t)threads > njobs) threads = (int)njobs;
+    ora_sample_t s;
+    memset(&s, 0, sizeof s);
+    s.t = t;
+    s.ls = ls;
+    s.m0s = m0s;
+    s.step = step;
+    s.njobs = njobs;
+    atomic_init(&s.next, 0);
+    s.logical = logical;
+    s.candidates = candidates;
+    pthread_t *tid = malloc(threads * sizeof(pthread_t));
+    for (int i = 0; i < threads; ++i) pthread_create(&tid[i], NULL, sample_worker, &s);
+    for (int i = 0; i < threads; ++i) pthread_join(tid[i], NULL);
+    free(tid);
     return 0;
 }
 

@@ -36,6 +36,8 @@ def _lib() -> ctypes.CDLL:
     lib.hss_oracle_search.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                       u64p, u64p, u64p, u64p, ctypes.POINTER(OracleHit),
                                       ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+    lib.hss_oracle_sample.argtypes = [ctypes.c_void_p, u64p, u64p, ctypes.c_uint64, ctypes.c_uint32,
+                                      ctypes.c_int, u64p, u64p]
     return lib
 
 
@@ -69,6 +71,22 @@ class Oracle:
                 "processed": sum(proc), "r16": sum(r16), "hits": out_hits,
                 "row_candidates": cand, "row_products": prod, "row_processed": proc,
                 "row_r16": r16}
+
+    def sample(self, jobs: List[Tuple[int, int]], step: int, threads: Optional[int] = None) -> Dict:
+        """Strided sample for timing: job (l, m0) searches root l over
+        m = m0, m0 + step, ... <= limit.  Returns the logical pairs visited
+        and the candidates, per job and in total."""
+        n = len(jobs)
+        ls = (ctypes.c_uint64 * n)(*[l for l, _ in jobs])
+        m0s = (ctypes.c_uint64 * n)(*[m for _, m in jobs])
+        logical = (ctypes.c_uint64 * n)()
+        cand = (ctypes.c_uint64 * n)()
+        st = self.lib.hss_oracle_sample(self.tables, ls, m0s, step, n, threads or os.cpu_count() or 1,
+                                        logical, cand)
+        if st:
+            raise ValueError("invalid oracle sample arguments")
+        return {"pairs": sum(logical), "candidates": sum(cand), "job_pairs": list(logical),
+                "job_candidates": list(cand)}
 
     def close(self):
         if self.tables:

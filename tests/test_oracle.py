@@ -92,3 +92,15 @@ def test_oracle_detects_planted_error(built):
         a = o.search(500, 531)["candidates"]
         b = o.search(500, 530)["candidates"]
     assert a == 141046 and b != a
+
+
+def test_strided_sample_partitions_rows(built):
+    """The strided sample used to time the CPU search on a bounded share of a
+    batch: the offsets 0..step-1 of a row add up to the whole row."""
+    with Oracle(5000) as o:
+        whole = o.search(1853, 1856, threads=4)
+        jobs = [(l, l + k) for l in range(1853, 1857) for k in range(3)]
+        part = o.sample(jobs, 3, threads=4)
+        assert part["pairs"] == whole["pairs"]
+        assert part["candidates"] == whole["candidates"]
+        assert o.sample([(l, l) for l in range(1853, 1857)], 1)["candidates"] == whole["candidates"]
