@@ -406,6 +406,7 @@ int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint3
     if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
     if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
     if (ctrl[3] & 4u) return fail(h, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+    if (ctrl[3] & ~7u) return fail(h, HSS_ERR_OVERFLOW, "a device index check failed (an event index out of range)");
     uint32_t nh = std::min(ctrl[0], h->hit_cap);
     hits->resize(nh);
     if (nh) HSS_CUDA(h, cudaMemcpy(hits->data(), h->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));

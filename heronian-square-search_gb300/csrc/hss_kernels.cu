@@ -132,6 +132,22 @@ __host__ __device__ __forceinline__ uint32_t pow4_mod(uint32_t x, uint32_t m) {
     return s * s % m;
 }
 
+// Index checks of the event paths: an index outside its buffer is recorded
+// (kErrIndex in the launch's error word, which the host reports as an
+// error) and the access is skipped.
+constexpr unsigned int kErrIndex = 0x100u;
+
+__device__ __forceinline__ bool index_ok(uint32_t i, uint32_t n, unsigned int* err) {
+    if (i < n) return true;
+    atomicOr(err, kErrIndex);
+    return false;
+}
+
+__device__ __forceinline__ uint32_t tab_at(const uint8_t* tab, uint32_t base, uint32_t i, uint32_t n,
+                                           unsigned int* err) {
+    return index_ok(i, n, err) ? tab[base + i] : 0u;
+}
+
 // ----------------------------------------------------------- 256-bit check
 
 // Heron recheck (done on the host by the reference's CPU search,
@@ -436,22 +452,46 @@ __device__ __forceinline__ bool pair_dual(const PairCtx& c) { return (c.m >> 31)
 // product, count one orientation, or test one orientation for a hit.
 constexpr uint32_t kExCount = 0, kExOrient = 1, kExHit = 2;
 
+// Appends one exact work item (a, b: exact-value indices; for shared-prime
+// pairs, list entries) to the global exact queue.
+__device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t kind, uint32_t a, uint32_t b, uint32_t l,
+                                           uint32_t m, uint32_t row, bool shared_prime) {
+    unsigned int idx = atomicAdd(buf.exact_count, 1u);
+    if (idx < buf.exact_cap)
+        buf.exact_queue[idx] = ExactItem{kind | (shared_prime ? 16u : 0u), a, b, l, m, row, 0u, 0u};
+    else
+        atomicOr(buf.error_flags, 4u);
+}
+
+// Where an event's exact work goes: the exact-value indices (a, b) of its two
+// values, the pair and its row, and whether the values are shared-prime
+// list entries.  Passed by value, so no pointer to a caller's locals crosses
+// an out-of-line call.
+struct EventSink {
+    const LaunchBuffers* buf;
+    uint32_t a, b, l, m, row, shared_prime;
+};
+
+__device__ __forceinline__ void sink_push(const EventSink& s, uint32_t kind) {
+    push_exact(*s.buf, kind, s.a, s.b, s.l, s.m, s.row, s.shared_prime != 0);
+}
+
 // Work of one event (one lane), in float and 32-bit integer arithmetic only:
 // an undecided product is queued for exact counting; the (y, x) orientation
 // of a non-dual product whose both orientations passed is decided and
 // counted; every counted orientation whose z passed mod 9360 goes through the
 // mod-625 / mod-119 filters and the fourth-root filter, and survivors are
-// queued for the exact hit test.  push(kind | p << 2 | o << 3) queues work.
+// queued for the exact hit test (kind | p << 2 | o << 3).
 //
 // With `slots` (warp-queue paths) the root filter of up to kReqPerLane terms
-// is left to the warp as requests (*nreq of them); orientations that the lane
-// itself found possible are returned in *passed (bit 2p + o) instead of being
-// queued, so that the caller queues each orientation once.
-template <class PushFn>
-__device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a, uint32_t arw, uint32_t aiw,
-                                              const HotRec& b, const PairCtx& c, uint32_t n_limit,
-                                              const uint8_t* tab, Acc& acc, PushFn push, RootReq* slots = nullptr,
-                                              uint32_t* nreq = nullptr, uint32_t* passed = nullptr) {
+// is left to the warp as requests; orientations that the lane itself found
+// possible are returned instead of being queued, so that the caller queues
+// each orientation once.  Returns (candidates, mod-16 survivors, requests
+// left, possible orientations as bits 2p + o).
+__device__ __noinline__ uint4 general_event(uint32_t flags, AlphaHot a, uint32_t arw, uint32_t aiw, HotRec b,
+                                            PairCtx c, uint32_t n_limit, const uint8_t* tab, EventSink sink,
+                                            RootReq* slots) {
+    uint32_t cand = 0, r16 = 0, nreq = 0, passed = 0;
     const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
     const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
     const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
@@ -463,7 +503,7 @@ __device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a,
         const uint32_t f = (flags >> (4 * p)) & 15u;
         if (!f) continue;
         if (f & kEvU) {
-            push(kExCount | (uint32_t)p << 2);
+            sink_push(sink, kExCount | (uint32_t)p << 2);
             continue;
         }
         const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
@@ -479,17 +519,18 @@ __device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a,
             const Window w = window(t, c);
             if (full) {
                 if (w.und) {
-                    push(kExOrient | (uint32_t)p << 2 | (uint32_t)o << 3);
+                    sink_push(sink, kExOrient | (uint32_t)p << 2 | (uint32_t)o << 3);
                     continue;
                 }
-                acc.cand += (uint32_t)w.in1 + (uint32_t)w.in2;
+                cand += (uint32_t)w.in1 + (uint32_t)w.in2;
             }
             const uint32_t dA = (o ? Y : X) % kModA;
             const bool neg = d < 0.f;
             const uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
             const uint32_t zA1 = sub_mod(sA, tA, kModA), zA2 = add_mod(sA, tA, kModA);
-            const uint32_t m1 = w.in1 ? tab[kTabA + zA1] : 0u, m2 = w.in2 ? tab[kTabA + zA2] : 0u;
-            if (full) acc.r16 += (m1 & 1u) + (m2 & 1u);
+            const uint32_t m1 = w.in1 ? tab_at(tab, kTabA, zA1, kModA, sink.buf->error_flags) : 0u;
+            const uint32_t m2 = w.in2 ? tab_at(tab, kTabA, zA2, kModA, sink.buf->error_flags) : 0u;
+            if (full) r16 += (m1 & 1u) + (m2 & 1u);
             if (!((m1 | m2) & sel)) continue;
             uint32_t xB, yB, xC, yC;
             coord_res(arw, aiw, b.rre, b.rim, 1, p, xB, yB);
@@ -502,36 +543,106 @@ __device__ __forceinline__ void process_event(uint32_t flags, const AlphaHot& a,
                 if (!(mm & sel)) continue;
                 const uint32_t zB = term ? add_mod(sB, tB, kModB) : sub_mod(sB, tB, kModB);
                 const uint32_t zC = term ? add_mod(sC, tC, kModC) : sub_mod(sC, tC, kModC);
-                if (flag5 ? zB != 0 : !tab[kTabB + zB]) continue;
-                if (!tab[kTabC + zC]) continue;
+                if (flag5 ? zB != 0 : !tab_at(tab, kTabB, zB, kModB, sink.buf->error_flags)) continue;
+                if (!tab_at(tab, kTabC, zC, kModC, sink.buf->error_flags)) continue;
                 const float zf = term ? c.sf + t : c.sf - t;
                 uint32_t nlo, nhi;
                 root_window(zf, c, n_limit, nlo, nhi);
                 const uint32_t zres = (term ? zA2 : zA1) | (zB << kShiftB) | (zC << kShiftC);
-                if (slots && *nreq < kReqPerLane)
-                    slots[(*nreq)++] = RootReq{nlo, nhi, zres, 2u * (uint32_t)p + (uint32_t)o};
+                if (slots && nreq < kReqPerLane)
+                    slots[nreq++] = RootReq{nlo, nhi, zres, 2u * (uint32_t)p + (uint32_t)o};
                 else if (root_scan(nlo, nhi, zres))
                     hit_possible = true;
             }
             if (hit_possible) {
                 if (slots)
-                    *passed |= 1u << (2 * p + o);
+                    passed |= 1u << (2 * p + o);
                 else
-                    push(kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
+                    sink_push(sink, kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
             }
         }
     }
+    return make_uint4(cand, r16, nreq, passed);
 }
 
-// Appends one exact work item (a, b: exact-value indices; for shared-prime
-// pairs, list entries) to the global exact queue.
-__device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t kind, uint32_t a, uint32_t b, uint32_t l,
-                                           uint32_t m, uint32_t row, bool shared_prime) {
-    unsigned int idx = atomicAdd(buf.exact_count, 1u);
-    if (idx < buf.exact_cap)
-        buf.exact_queue[idx] = ExactItem{kind | (shared_prime ? 16u : 0u), a, b, l, m, row, 0u, 0u};
-    else
-        atomicOr(buf.error_flags, 4u);
+// One deep unit of an event: orientation o of product p (p = 1: alpha *
+// conj(beta)) was counted by the filter loop and its z passed the mod-kModA
+// table for some term.  The coordinate D of the orientation is
+// u + v, u - v or v - u with u, v = (ar br, ai bi) for o = 0 and
+// (ar bi, ai br) for o = 1; everything is computed branch-free in p and o, so
+// lanes holding different units run one instruction stream.  Terms that pass
+// the mod-625 and mod-119 tables go to the root filter: left as requests in
+// `slots` while there is room, else scanned here; returns true when such a
+// scan found a possible root.
+__device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot& a, uint32_t arw, uint32_t aiw,
+                                          const HotRec& b, const PairCtx& c, uint32_t n_limit, const uint8_t* tab,
+                                          RootReq* slots, uint32_t& nreq, unsigned int* err) {
+    const bool plus = o != p;
+    const float fu = o ? a.re * b.im : a.re * b.re;
+    const float fv = o ? a.im * b.re : a.im * b.im;
+    const float d = plus ? fu + fv : (o ? fv - fu : fu - fv);
+    const float t = fabsf(d);
+    const bool neg = d < 0.f;
+    // D mod M from the packed residues of one field, signed by d
+    auto field = [&](uint32_t wa, uint32_t wai, uint32_t wb, uint32_t wbi, uint32_t M) {
+        const uint32_t u = o ? wa * wbi : wa * wb, v = o ? wai * wb : wai * wbi;
+        const uint32_t r = (plus ? u + v : (o ? v + M * M - u : u + M * M - v)) % M;
+        return neg ? (r ? M - r : 0u) : r;
+    };
+    const uint32_t tA = field(a.ra & 0x7FFFFFFFu, a.ia, b.rre & kMaskA, b.rim & kMaskA, kModA);
+    const Window w = window(t, c);
+    const uint32_t sA = c.sres & kMaskA, sB = (c.sres >> kShiftB) & kMaskB, sC = (c.sres >> kShiftC) & kMaskC;
+    const bool flag5 = (c.sres >> 31) != 0;
+    const uint32_t sel = flag5 ? 4u : 2u;
+    const uint32_t zA1 = sub_mod(sA, tA, kModA), zA2 = add_mod(sA, tA, kModA);
+    const uint32_t m1 = w.in1 ? tab_at(tab, kTabA, zA1, kModA, err) : 0u;
+    const uint32_t m2 = w.in2 ? tab_at(tab, kTabA, zA2, kModA, err) : 0u;
+    const uint32_t tB = field((arw >> kShiftB) & kMaskB, (aiw >> kShiftB) & kMaskB, (b.rre >> kShiftB) & kMaskB,
+                              (b.rim >> kShiftB) & kMaskB, kModB);
+    const uint32_t tC = field((arw >> kShiftC) & kMaskC, (aiw >> kShiftC) & kMaskC, (b.rre >> kShiftC) & kMaskC,
+                              (b.rim >> kShiftC) & kMaskC, kModC);
+    bool hit = false;
+#pragma unroll
+    for (int term = 0; term < 2; ++term) {
+        if (!((term ? m2 : m1) & sel)) continue;
+        const uint32_t zB = term ? add_mod(sB, tB, kModB) : sub_mod(sB, tB, kModB);
+        const uint32_t zC = term ? add_mod(sC, tC, kModC) : sub_mod(sC, tC, kModC);
+        if (flag5 ? zB != 0 : !tab_at(tab, kTabB, zB, kModB, err)) continue;
+        if (!tab_at(tab, kTabC, zC, kModC, err)) continue;
+        uint32_t nlo, nhi;
+        root_window(term ? c.sf + t : c.sf - t, c, n_limit, nlo, nhi);
+        const uint32_t zres = (term ? zA2 : zA1) | (zB << kShiftB) | (zC << kShiftC);
+        if (slots && nreq < kReqPerLane)
+            slots[nreq++] = RootReq{nlo, nhi, zres, 2u * p + o};
+        else if (!hit && root_scan(nlo, nhi, zres))
+            hit = true;
+    }
+    return hit;
+}
+
+// Work of one event: events with an undecided product or a non-dual product
+// whose both orientations passed take the general path; the others are a set
+// of deep units (one bit per counted orientation whose z passed mod kModA).
+// Returns (candidates, mod-16 survivors, requests left, possible
+// orientations) as general_event does.
+__device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a, uint32_t arw, uint32_t aiw,
+                                               const HotRec& b, const PairCtx& c, uint32_t n_limit,
+                                               const uint8_t* tab, const EventSink& sink, RootReq* slots) {
+    if (flags & ((kEvU | kEvB) * 0x11u)) return general_event(flags, a, arw, aiw, b, c, n_limit, tab, sink, slots);
+    uint32_t units = ((flags & kEvDx) ? 1u : 0u) | ((flags & kEvDy) ? 2u : 0u) |
+                     ((flags & (kEvDx << 4)) ? 4u : 0u) | ((flags & (kEvDy << 4)) ? 8u : 0u);
+    uint32_t nreq = 0, passed = 0;
+    while (units) {
+        const uint32_t u = __ffs(units) - 1;
+        units &= units - 1;
+        if (deep_unit(u >> 1, u & 1u, a, arw, aiw, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags)) {
+            if (slots)
+                passed |= 1u << u;
+            else
+                sink_push(sink, kExHit | (u >> 1) << 2 | (u & 1u) << 3);
+        }
+    }
+    return make_uint4(0u, 0u, nreq, passed);
 }
 
 // Event handler of the cached path: record j against the row value whose
@@ -543,12 +654,9 @@ __device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t ki
 __device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
                                               uint32_t j, uint32_t l, uint32_t row, const uint8_t* tab,
                                               uint32_t limit, const LaunchBuffers* buf, RootReq* slots = nullptr) {
-    Acc acc{0, 0, 0, 0, 0, 0};
-    uint32_t nreq = 0, passed = 0;
-    process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
-                  [&](uint32_t kind) { push_exact(*buf, kind, ka, j, l, pair_m(c), row, false); }, slots, &nreq,
-                  &passed);
-    return make_uint2(acc.cand | (nreq << 16) | (passed << 20), acc.r16);
+    const EventSink sink{buf, ka, j, l, pair_m(c), row, 0u};
+    const uint4 r = process_event(flags, a, abc.x, abc.y, b, c, limit, tab, sink, slots);
+    return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
 
 // Queues the exact hit test of each orientation in `tags` (bit 2p + o).
@@ -710,8 +818,8 @@ __device__ __forceinline__ bool queue_push(uint64_t* q, uint32_t& count, bool ha
 // queues the exact hit test of each possible orientation of the lane's event.
 // All 32 lanes must call it.
 template <class Handler, class HitFn>
-__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, RootReq* wreq, Handler handle,
-                                      HitFn hit) {
+__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, RootReq* wreq, unsigned int* err,
+                                      Handler handle, HitFn hit) {
     __syncwarp();
     const uint32_t lane = threadIdx.x & 31;
     uint64_t ev = 0;
@@ -727,7 +835,11 @@ __device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, 
     while (todo) {
         const uint32_t src = __ffs(todo) - 1;
         todo &= todo - 1;
-        const uint32_t cnt = __shfl_sync(kFull, nreq, src);
+        uint32_t cnt = __shfl_sync(kFull, nreq, src);
+        if (cnt > kReqPerLane) {
+            if (lane == 0) atomicOr(err, kErrIndex);
+            cnt = kReqPerLane;
+        }
         for (uint32_t r = 0; r < cnt; ++r) {
             const RootReq rq = wreq[src * kReqPerLane + r];
             if (root_scan_warp(rq, lane) && lane == src) passed |= 1u << rq.tag;
@@ -789,6 +901,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
     const uint32_t excl = incl - mine;
     auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
+        if (!index_ok(k, na, buf.error_flags) || !index_ok(slot, 32 * kRootsPerLane, buf.error_flags)) return 0u;
         const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], s_abc[k], cache.hot[j], wctx[slot], a0 + k, j,
                                      (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
         acc.cand += r.x & 0xFFFFu;
@@ -830,10 +943,10 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
             if (live) flags = eval_fast<DUAL>(a, b.re, b.im, bra, bia, cb, c, s_tab, acc);
-            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, handle, hit);
+            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
-    while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, handle, hit);
+    while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
 }
 
 template <int NT, int MINB>
@@ -1116,13 +1229,10 @@ __device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc
                                               PairCtx c, uint32_t ka, uint32_t kb, uint32_t l, uint32_t row,
                                               const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf,
                                               RootReq* slots = nullptr) {
-    Acc acc{0, 0, 0, 0, 0, 0};
-    uint32_t nreq = 0, passed = 0;
     const HotRec b{bh.re, bh.im, bbc.x | (bh.ra & kCentralBit), bbc.y};
-    process_event(flags, a, abc.x, abc.y, b, c, limit, tab, acc,
-                  [&](uint32_t kind) { push_exact(*buf, kind, ka, kb, l, pair_m(c), row, true); }, slots, &nreq,
-                  &passed);
-    return make_uint2(acc.cand | (nreq << 16) | (passed << 20), acc.r16);
+    const EventSink sink{buf, ka, kb, l, pair_m(c), row, 1u};
+    const uint4 r = process_event(flags, a, abc.x, abc.y, b, c, limit, tab, sink, slots);
+    return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
 
 // Splits the merged terms of (l, m) into two groups (largest terms first,
@@ -1360,6 +1470,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             const float rcp = 1.0f / (float)nb;
             auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+                if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
                 const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c,
                                              ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
                 acc.cand += r.x & 0xFFFFu;
@@ -1393,9 +1504,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                                                     c, s_tab, acc);
                 }
                 if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags)))
-                    drain(q, qn, 32, wreq, handle, hit);
+                    drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
             }
-            while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, handle, hit);
+            while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
             __syncwarp();
         }
         if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
