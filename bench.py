@@ -12,18 +12,24 @@ over that batch through the C ABI (hss_search).  Metric: logical pairs/s.
             items' host-to-device copy from pinned memory, the kernels, and the
             device-to-host read of counters and hits
   plain     the same batch on the plain path (the reference's launch shape)
+  serving   a seeded Poisson stream of interval requests (lengths log-uniform
+            in [1, 4096] roots, uniform starts) through the serving loop, with
+            p50/p99 latency, against the same requests run one at a time
   roofline  integer-op model of the dominant (persistent) kernel against a
-            measured INT32 throughput probe
-  cpu_baseline  the CPU oracle on a bounded sample of the same batch
+            measured INT32 throughput probe; DRAM traffic from an ncu capture
+  cpu_baseline  the CPU oracle on a bounded strided sample of the same batch
 
 Multi-GPU: replicas.  Rank r searches its own 512-root batch starting at
 7,500,000 + 512 r (weak scaling); there is no collective on the data path.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--no-plain] [--no-cpu] [--no-serving]
 """
 import argparse
 import json
+import math
 import os
+import random
 import statistics
 import subprocess
 import sys
@@ -40,10 +46,21 @@ FIRST = 7_500_000
 ROWS = 512
 METRIC = "logical (l,m) pairs/s at LIMIT 1e7 on 1 GB300, batched vs plain; p50/p99 latency"
 UNIT = "pairs/s"
-# CPU sample: 16 root rows of the batch, one per host thread of the oracle
-SAMPLE_ROWS = [7500000, 7500001, 7500002, 7500003] + list(range(7500008, 7500020))
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC = ROOT / "profiles" / "traffic.json"
+
+# CPU sample of the batch: 64 jobs (rows spread over the batch, both
+# parities), each job one row over every STEP-th m; one job per host thread
+# at a time.
+SAMPLE_JOBS = 64
+SAMPLE_STEP = 8          # cpu_baseline of our arm (about 20 s on 16 Arm cores)
+REFERENCE_STEP = 16      # each step of the reference arm (about 10 s)
+
+# serving stream
+SERVE_SEED = 5
+SERVE_REQUESTS = 12
+SERVE_RATE = 10.0        # requests per second (Poisson)
+SERVE_MAX_LEN = 4096     # lengths log-uniform in [1, SERVE_MAX_LEN] roots
 
 
 def logical_pairs(first, last, limit=LIMIT):
@@ -91,80 +108,125 @@ class Clocks:
             if len(f) < 9:
                 continue
             try:
-                rows.append((float(f[1]), float(f[2]), f[5:9]))
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5:9]))
             except ValueError:
                 continue
         os.unlink(self.file.name)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, flags in rows for i, v in enumerate(flags) if v == "Active"})
-        loaded = [sm for sm, _, _ in rows]
-        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx for _, mx, _ in rows),
-                "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for _, _, _, flags in rows for i, v in enumerate(flags) if v == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_sample(rows=SAMPLE_ROWS):
-    """The oracle (a restatement of the reference's CPU search) on the sample
-    rows, all host threads; returns (pairs/s, seconds, threads, kind)."""
+def sample_jobs(first=FIRST, rows=ROWS, jobs=SAMPLE_JOBS, step=SAMPLE_STEP):
+    """Job i: row first + 8i + (i mod 2) (spread over the batch, alternating
+    parity), m = l + (i mod step), then every step-th m."""
+    out = []
+    stride = max(rows // jobs, 1)
+    for i in range(jobs):
+        l = first + min(stride * i + (i % 2), rows - 1)
+        out.append((l, l + (i % step)))
+    return out
+
+
+def cpu_sample(step, jobs=SAMPLE_JOBS):
+    """The oracle (a restatement of the reference's CPU search) on a strided
+    sample of the batch with all host threads; returns (pairs/s, seconds,
+    threads, kind, pairs)."""
     from oracle import Oracle
     threads = os.cpu_count() or 1
-    pairs = sum(LIMIT - l + 1 for l in rows)
     with Oracle(LIMIT) as o:
         t = time.time()
-        for i in range(0, len(rows), threads):
-            _run_rows(o, rows[i:i + threads])
+        r = o.sample(sample_jobs(jobs=jobs, step=step), step, threads=threads)
         sec = time.time() - t
-    return pairs / sec, sec, min(threads, len(rows)), "port"
-
-
-def _run_rows(o, rows):
-    """One host thread per row (the reference's workers also take one row
-    at a time, search_v18.cpp:311-327)."""
-    import threading
-    errors = []
-
-    def work(l):
-        try:
-            o.search(l, l, threads=1)
-        except Exception as e:  # pragma: no cover
-            errors.append(e)
-
-    ts = [threading.Thread(target=work, args=(l,)) for l in rows]
-    for t in ts:
-        t.start()
-    for t in ts:
-        t.join()
-    if errors:
-        raise errors[0]
+    return r["pairs"] / sec, sec, min(threads, jobs), "port", r["pairs"]
 
 
 def reference_arm(args, rank, world):
     if rank != 0:
         return 0
-    from oracle import build as build_oracle
+    from oracle import Oracle, build as build_oracle
     build_oracle()
-    for _ in range(args.warmup):
-        pass  # the CPU sample has no warm-up state beyond the prepared tables
+    threads = os.cpu_count() or 1
+    jobs = sample_jobs(step=REFERENCE_STEP)
     vals, secs = [], []
-    for _ in range(args.steps):
-        v, sec, cores, kind = cpu_sample()
-        vals.append(v)
-        secs.append(sec)
+    pairs = 0
+    with Oracle(LIMIT) as o:
+        for _ in range(args.warmup):
+            o.sample(jobs[:threads], REFERENCE_STEP * 64, threads=threads)
+        for _ in range(args.steps):
+            t = time.time()
+            r = o.sample(jobs, REFERENCE_STEP, threads=threads)
+            sec = time.time() - t
+            pairs = r["pairs"]
+            vals.append(pairs / sec)
+            secs.append(sec)
     value = statistics.mean(vals)
+    sample = (f"{len(jobs)} jobs spread over the batch, each one row over every {REFERENCE_STEP}th m "
+              f"({pairs} logical pairs per step), {min(threads, len(jobs))} host threads")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic (the search interval itself; no dataset)",
             "config": {"workload": f"LIMIT={LIMIT}, root edges {FIRST}..{FIRST + ROWS - 1} (one reference batch); "
-                                   f"each step a sample of {len(SAMPLE_ROWS)} of its rows",
-                       "limit": LIMIT, "sample_rows": SAMPLE_ROWS},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
-                             "sample": f"{len(SAMPLE_ROWS)} rows of the batch ({sum(LIMIT - l + 1 for l in SAMPLE_ROWS)} "
-                                       "logical pairs), one row per host thread"},
+                                   "each step a strided sample of it on the host cores",
+                       "limit": LIMIT, "sample_step": REFERENCE_STEP, "sample_jobs": len(jobs)},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": min(threads, len(jobs)), "kind": "port",
+                             "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+def serving(s, seed=SERVE_SEED, n_req=SERVE_REQUESTS, rate=SERVE_RATE, max_len=SERVE_MAX_LEN):
+    """Seeded Poisson stream through the serving loop, then the same requests
+    one at a time (hss_search, batched path).  Latency = finish - submit."""
+    rng = random.Random(seed)
+    reqs, t = [], 0.0
+    for _ in range(n_req):
+        t += rng.expovariate(rate)
+        length = min(max(int(round(math.exp(rng.uniform(0.0, math.log(max_len))))), 1), max_len)
+        first = rng.randint(1, LIMIT - length + 1)
+        reqs.append((t, first, first + length - 1))
+    s.serve_start()
+    ids = []
+    t0 = time.time()
+    for at, a, b in reqs:
+        delay = t0 + at - time.time()
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(s.submit(a, b))
+    done = [s.wait(i) for i in ids]
+    makespan = time.time() - t0
+    s.serve_stop()
+    lat = sorted((d["finished_ns"] - d["submitted_ns"]) / 1e6 for d in done)
+    pairs = sum(logical_pairs(a, b) for _, a, b in reqs)
+    # one at a time, arrivals replayed: a request starts when it has arrived
+    # and the previous one has finished (service times measured)
+    seq_lat, clock, same = [], 0.0, True
+    for (at, a, b), d in zip(reqs, done):
+        t1 = time.time()
+        r = s.search(a, b)
+        svc = time.time() - t1
+        clock = max(clock, at) + svc
+        seq_lat.append(1e3 * (clock - at))
+        same &= all(r.counts[k] == d["counts"][k] for k in ("pairs", "candidates", "products", "processed"))
+        same &= sorted(r.hits) == sorted(d["hits"])
+    seq_lat.sort()
+
+    def pct(v, q):
+        return v[min(len(v) - 1, int(math.ceil(q * len(v))) - 1)]
+
+    return {"requests": n_req, "rate_per_s": rate, "lengths": f"log-uniform [1, {max_len}] roots", "seed": seed,
+            "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
+            "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+            "one_at_a_time": {"pairs_per_s": pairs / (clock - reqs[0][0]) if clock > reqs[0][0] else None,
+                              "p50_ms": pct(seq_lat, 0.5), "p99_ms": pct(seq_lat, 0.99)},
+            "results_same_alone_and_in_mix": bool(same),
+            "note": "offered load exceeds device capacity (mean request about 2.5e9 pairs); "
+                    "latency includes queueing; p99 of 12 requests is their maximum"}
 
 
 def our_arm(args, rank, world, local_rank):
@@ -187,17 +249,16 @@ def our_arm(args, rank, world, local_rank):
         dist.barrier()
     steps = []
     with Clocks(local_rank) as clk:
-        wall0 = time.time()
         for _ in range(args.steps):
             t = time.time()
             r = s.search(first, last)
             steps.append((r, time.time() - t))
-        wall = time.time() - wall0
     if dist:
         dist.barrier()
     clocks = clk.summary()
     dev_ms = sum(r.counts["kernel_ms"] for r, _ in steps) / args.steps
     main_ms = sum(r.counts["main_ms"] for r, _ in steps) / args.steps
+    merged_ms = sum(r.counts["merged_ms"] for r, _ in steps) / args.steps
     e2e_ms = 1e3 * sum(w for _, w in steps) / args.steps
     c = steps[-1][0].counts
     if dist:
@@ -208,57 +269,66 @@ def our_arm(args, rank, world, local_rank):
     if rank != 0:
         s.close()
         return 0
-    # plain path, same batch, one step (the reference's launch shape)
     plain = s.search(first, last, mode="plain") if not args.no_plain else None
+    serve = serving(s) if not args.no_serving else None
     # integer roofline of the persistent kernel
-    peak_ops = 0.0
     import ctypes
     lib = hss.load_library()
-    v, ms = ctypes.c_double(), ctypes.c_double()
-    if lib.hss_int32_peak(local_rank, ctypes.byref(v), ctypes.byref(ms)) == 0:
-        peak_ops = v.value
+    peak, probe_ms = ctypes.c_double(), ctypes.c_double()
+    peak_ops = peak.value if lib.hss_int32_peak(local_rank, ctypes.byref(peak), ctypes.byref(probe_ms)) == 0 else 0.0
     q = c["processed"] - c["merged"]
     p = c["products"] - c["merged_products"]
     cc = c["candidates"] - c["merged_candidates"]
     rr = c["r16"] - c["merged_r16"]
-    ops = model_ops(q, p, cc, rr)
-    achieved = ops / (main_ms * 1e-3) / 1e9
-    traffic = None
+    achieved = model_ops(q, p, cc, rr) / (main_ms * 1e-3) / 1e9
+    traffic = hbm = None
     if TRAFFIC.exists():
-        traffic = json.loads(TRAFFIC.read_text()).get("batched_kernel_bytes_per_launch")
+        t = json.loads(TRAFFIC.read_text())
+        traffic = t.get("batched_kernel_bytes_per_launch")
+        if traffic and PEAKS.exists():
+            gbs = traffic / (main_ms * 1e-3) / 1e9
+            peak_gbs = json.loads(PEAKS.read_text()).get("hbm_gbs")
+            hbm = {"achieved_gbs": gbs, "peak_gbs": peak_gbs, "frac": gbs / peak_gbs if peak_gbs else None,
+                   "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     cpu = None
-    if rank == 0 and not args.no_cpu:
-        cv, csec, ccores, kind = cpu_sample()
+    if not args.no_cpu:
+        cv, csec, ccores, kind, cpairs = cpu_sample(SAMPLE_STEP)
         cpu = {"value": cv, "unit": UNIT, "cores": ccores, "kind": kind,
-               "sample": f"{len(SAMPLE_ROWS)} rows of the batch ({sum(LIMIT - l + 1 for l in SAMPLE_ROWS)} logical "
-                         f"pairs, {csec:.1f} s), one row per host thread, oracle restating src/search_v18.cpp"}
+               "sample": f"{SAMPLE_JOBS} jobs spread over the batch, each one row over every {SAMPLE_STEP}th m "
+                         f"({cpairs} logical pairs, {csec:.1f} s), one job per host thread at a time; "
+                         "oracle restating src/search_v18.cpp"}
     value = world * pairs / (dev_ms * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int64",
+        "vs_baseline": None, "dtype": "int32",
         "data": "synthetic (the search interval itself; no dataset)",
         "config": {"workload": f"LIMIT={LIMIT}, root edges {first}..{last} per GPU (one reference batch)",
                    "limit": LIMIT, "roots_per_gpu": ROWS, "pairs_per_gpu": pairs, "mode": "batched",
                    "parallelism": f"replicas{world}",
-                   "l2": "inputs larger than L2: the m-side factor cache streamed per step is ~0.5 GB"},
+                   "arithmetic": "int32 residues and f32 bounds in the filter loop; i128 exact path, u256 recheck",
+                   "l2": "inputs larger than L2: each step streams the m-side factor records (about 0.4 GB)"},
         "e2e": {"value": world * pairs / (e2e_ms * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": c["h2d_bytes"], "d2h_bytes_per_step": c["d2h_bytes"]},
+        "candidates_per_s": world * c["candidates"] / (dev_ms * 1e-3),
+        "kernels_ms": {"persistent": main_ms, "shared_prime_and_exact": merged_ms},
         "plain": None if plain is None else {
             "value": pairs / (plain.counts["kernel_ms"] * 1e-3), "unit": UNIT,
             "ms_per_step": plain.counts["kernel_ms"],
-            "batched_over_plain": plain.counts["kernel_ms"] / dev_ms},
+            "batched_over_plain": plain.counts["kernel_ms"] / dev_ms,
+            "counts_equal": all(plain.counts[k] == c[k] for k in ("pairs", "candidates", "products"))},
+        "serving": serve,
         "counts": {k: c[k] for k in ("pairs", "processed", "products", "candidates", "r16", "exact", "merged",
                                      "hits")},
         "roofline": {"bound": "int32", "achieved": achieved, "peak": peak_ops / 1e9, "unit": "Gop/s",
                      "frac": achieved / (peak_ops / 1e9) if peak_ops else None, "traffic": traffic,
                      "model": "16 Q + 64 P + 32 C + 160 R over the persistent kernel's pairs",
-                     "kernel_ms": main_ms, "peak_source": "measured INT32 probe kernel (hss_int32_peak)"},
+                     "kernel_ms": main_ms, "peak_source": "measured INT32 probe kernel (hss_int32_peak)",
+                     "hbm": hbm},
         "cpu_baseline": cpu,
         "gpu_launches": sum(r.counts["launches"] for r, _ in steps),
         "clocks": clocks,
-        "prep": {"open_seconds": open_s, "host_cache_seconds": info["prep_seconds"],
-                 "records": info["records"]},
+        "prep": {"open_seconds": open_s, "host_cache_seconds": info["prep_seconds"], "records": info["records"]},
     }
     print(json.dumps(line))
     s.close()
@@ -273,6 +343,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))

@@ -279,6 +279,42 @@ int upload_row_info(hss_t* h, const std::vector<uint64_t>& ls) {
     return HSS_OK;
 }
 
+// Captures the stream work of `enqueue` in a CUDA graph and launches it.  The
+// handle keeps one executable graph and updates it in place from each new
+// capture (item count, grid and buffer sizes change between calls); when the
+// update is refused, the graph is instantiated again.
+template <class Enqueue>
+int run_captured(hss_t* h, Enqueue enqueue) {
+    HSS_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int s = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(h->stream, &g);
+    if (s || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (s) return s;
+        return fail(h, HSS_ERR_CUDA, std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));
+    }
+    bool updated = false;
+    if (h->graph_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(h->graph_exec, g, &info) == cudaSuccess) {
+            updated = true;
+        } else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(h->graph_exec);
+            h->graph_exec = nullptr;
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    if (!updated) e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, HSS_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    HSS_CUDA(h, cudaGraphLaunch(h->graph_exec, h->stream));
+    ++h->graph_launches;
+    ++h->call_graphs;
+    return HSS_OK;
+}
+
 // Launches the batched sequence for a set of rows whose shared-prime pairs
 // fit the queue: reset cursor/queue, items H2D, persistent kernel, shared-prime
 // kernel.  Counters accumulate into d_rows[index].
@@ -291,11 +327,6 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     size_t n_items = build_items(h, rows, nrows, &acap, (uint32_t)threads / 32 * 128);
     if (n_items == (size_t)-1) return HSS_ERR_MEMORY;
     if (n_items == 0) return HSS_OK;
-    HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
-                                h->stream));
-    h->h2d_bytes += n_items * sizeof(WorkItem);
-    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
-    HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
     cfg.min_blocks = h->opts.ctas_per_sm ? (int)h->opts.ctas_per_sm : (cfg.threads == 128 ? 4 : cfg.threads == 512 ? 1 : 2);
@@ -306,12 +337,26 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     LaunchBuffers b = buffers(h, 0);
     std::array<cudaEvent_t, 3> ev;
     if (int e = take_events(h, &ev)) return e;
-    HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
-    HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
-    HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
-    HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
-    HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
-    HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
+    // the group's stream work: items H2D, queue resets, the three kernels
+    auto enqueue = [&]() -> int {
+        HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
+                                    h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
+        HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
+        HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
+        return HSS_OK;
+    };
+    if (h->opts.use_graph) {
+        if (int e = run_captured(h, enqueue)) return e;
+    } else if (int e = enqueue()) {
+        return e;
+    }
+    h->h2d_bytes += n_items * sizeof(WorkItem);
     h->marks.push_back(ev);
     h->launches += 4;
     return HSS_OK;
@@ -376,6 +421,7 @@ int begin_call(hss_t* h, size_t rows) {
     h->events_used = 0;
     h->marks.clear();
     h->launches = 0;
+    h->call_graphs = 0;
     h->h2d_bytes = h->d2h_bytes = 0;
     return HSS_OK;
 }
@@ -577,6 +623,7 @@ void hss_close(hss_t* h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -656,6 +703,7 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     out->main_ms = main_ms;
     out->merged_ms = merged_ms;
     out->launches = h->launches;
+    out->graph_launches = h->call_graphs;
     out->h2d_bytes = h->h2d_bytes;
     out->d2h_bytes = h->d2h_bytes;
     for (size_t r = 0; r < rows; ++r) {
@@ -739,6 +787,7 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
     sum.main_ms = main_ms;
     sum.merged_ms = merged_ms;
     sum.launches = h->launches;
+    sum.graph_launches = h->call_graphs;
     sum.h2d_bytes = h->h2d_bytes;
     sum.d2h_bytes = h->d2h_bytes;
     size_t r = 0;

@@ -61,6 +61,11 @@ struct hss_ctx {
 
     std::mutex gpu_mu;  // serialises device work on the handle
 
+    // batched launch groups captured as a graph (opts.use_graph)
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_launches = 0;
+    uint32_t call_graphs = 0;  // graph launches of the current call
+
     // per-call accounting: event triples (before main kernel, after it,
     // after the shared-prime kernels) for every launch group
     std::vector<cudaEvent_t> event_pool;

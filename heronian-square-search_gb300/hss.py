@@ -39,7 +39,7 @@ class HssCounts(ctypes.Structure):
                 ("merged_products", ctypes.c_uint64), ("merged_candidates", ctypes.c_uint64),
                 ("merged_r16", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
                 ("d2h_bytes", ctypes.c_uint64), ("launches", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("graph_launches", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {name: getattr(self, name) for name, _ in self._fields_}

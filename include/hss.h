@@ -85,7 +85,7 @@ typedef struct {
     uint64_t h2d_bytes;          /* host-to-device bytes copied by the call */
     uint64_t d2h_bytes;          /* device-to-host bytes copied by the call */
     uint32_t launches;           /* kernels launched by the call */
-    uint32_t reserved;
+    uint32_t graph_launches;     /* CUDA graph launches of the call (opts.use_graph) */
 } hss_counts;
 
 /* A hit (l <= m <= n, gcd 1), with the signed 4A of the representation that
