@@ -149,6 +149,33 @@ int ensure_merged(hss_t* h, uint64_t n) {
     return HSS_OK;
 }
 
+// A launch group whose exact work outgrew the queue is incomplete: the queue
+// is enlarged 4x (up to 2^28 items) and the caller runs the whole call again.
+int grow_exact(hss_t* h) {
+    if (!h->exact_overflow) return HSS_ERR_OVERFLOW;
+    h->exact_overflow = false;
+    const uint64_t cap = (uint64_t)h->exact_cap * 4;
+    if (cap > (1ull << 28)) return HSS_ERR_OVERFLOW;
+    HSS_CUDA(h, cudaStreamSynchronize(h->stream));
+    device_free(h, h->d_exact);
+    h->d_exact = nullptr;
+    int s = device_alloc(h, &h->d_exact, (size_t)cap);
+    if (s) return s;
+    h->exact_cap = (uint32_t)cap;
+    return HSS_OK;
+}
+
+// Runs `call` again after enlarging the exact queue when it overflowed.
+template <class Call>
+int with_exact_retry(hss_t* h, Call call) {
+    for (int attempt = 0;; ++attempt) {
+        h->exact_overflow = false;
+        const int s = call();
+        if (s == HSS_ERR_OVERFLOW && h->exact_overflow && attempt < 3 && grow_exact(h) == HSS_OK) continue;
+        return s;
+    }
+}
+
 int ensure_items(hss_t* h, size_t n) {
     if (n > h->items_cap) {
         device_free(h, h->d_items);
@@ -315,6 +342,12 @@ int run_captured(hss_t* h, Enqueue enqueue) {
     return HSS_OK;
 }
 
+int search_locked(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* out, uint64_t* row_candidates,
+                  hss_hit* hits, uint32_t hit_cap, uint32_t* nhits);
+int search_many_locked(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uint32_t count, size_t rows,
+                       hss_counts* per_interval, hss_counts* total, hss_hit* hits, uint32_t hit_cap,
+                       uint32_t* nhits);
+
 // Launches the batched sequence for a set of rows whose shared-prime pairs
 // fit the queue: reset cursor/queue, items H2D, persistent kernel, shared-prime
 // kernel.  Counters accumulate into d_rows[index].
@@ -451,7 +484,10 @@ int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint3
     h->d2h_bytes += rows * sizeof(RowCounts) + sizeof ctrl;
     if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
     if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
-    if (ctrl[3] & 4u) return fail(h, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+    if (ctrl[3] & 4u) {
+        h->exact_overflow = true;
+        return fail(h, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+    }
     if (ctrl[3] & ~7u) return fail(h, HSS_ERR_OVERFLOW, "a device index check failed (an event index out of range)");
     uint32_t nh = std::min(ctrl[0], h->hit_cap);
     hits->resize(nh);
@@ -592,7 +628,7 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
     h->merged_cap = (uint32_t)kMergedCap;
     h->big_cap = 1u << 20;
-    h->exact_cap = 1u << 22;
+    h->exact_cap = 1u << 24;
     if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
         (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
         (s = device_alloc(h, &h->d_big, h->big_cap)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
@@ -679,6 +715,16 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     if (mode != HSS_MODE_PLAIN && mode != HSS_MODE_BATCHED) return fail(h, HSS_ERR_ARGUMENT, "unknown mode");
     std::lock_guard<std::mutex> lock(h->gpu_mu);
     HSS_CUDA(h, cudaSetDevice(h->device));
+    return with_exact_retry(h, [&] { return search_locked(h, first, last, mode, out, row_candidates, hits, hit_cap,
+                                                          nhits); });
+}
+
+}  // extern "C"
+
+namespace {
+
+int search_locked(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* out, uint64_t* row_candidates,
+                  hss_hit* hits, uint32_t hit_cap, uint32_t* nhits) {
     const size_t rows = (size_t)(last - first + 1);
     int s = begin_call(h, rows);
     if (s) return s;
@@ -717,6 +763,10 @@ int hss_search(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts* ou
     if (nhits) *nhits = nfound;
     return HSS_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tune_trial* trials,
                  uint32_t max_trials, uint32_t* ntrials) {
@@ -766,6 +816,18 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
     if (rows > UINT32_MAX) return fail(h, HSS_ERR_ARGUMENT, "too many rows");
     std::lock_guard<std::mutex> lock(h->gpu_mu);
     HSS_CUDA(h, cudaSetDevice(h->device));
+    return with_exact_retry(h, [&] {
+        return search_many_locked(h, firsts, lasts, count, rows, per_interval, total, hits, hit_cap, nhits);
+    });
+}
+
+}  // extern "C"
+
+namespace {
+
+int search_many_locked(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uint32_t count, size_t rows,
+                       hss_counts* per_interval, hss_counts* total, hss_hit* hits, uint32_t hit_cap,
+                       uint32_t* nhits) {
     int s = begin_call(h, rows);
     if (s) return s;
     std::vector<RowRef> refs;
@@ -819,7 +881,7 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
     return HSS_OK;
 }
 
-}  // extern "C"
+}  // namespace
 
 // ------------------------------------------------------------------ serving
 
@@ -880,14 +942,20 @@ void serve_loop(hss_t* h) {
         int s;
         {
             std::lock_guard<std::mutex> g(h->gpu_mu);
-            s = begin_call(h, rows.size());
-            if (!s) {
-                std::vector<uint64_t> ls(rows.size());
-                for (size_t i = 0; i < rows.size(); ++i) ls[i] = rows[i].l;
-                s = upload_row_info(h, ls);
-            }
-            if (!s) s = run_batched(h, rows);
-            if (!s) s = end_call(h, rows.size(), &ms, &found, &nfound);
+            s = with_exact_retry(h, [&] {
+                int r = begin_call(h, rows.size());
+                if (!r) {
+                    std::vector<uint64_t> ls(rows.size());
+                    for (size_t i = 0; i < rows.size(); ++i) ls[i] = rows[i].l;
+                    r = upload_row_info(h, ls);
+                }
+                if (!r) r = run_batched(h, rows);
+                if (!r) {
+                    found.clear();
+                    r = end_call(h, rows.size(), &ms, &found, &nfound);
+                }
+                return r;
+            });
         }
         std::lock_guard<std::mutex> lock(h->serve_mu);
         for (size_t i = 0; i < rows.size(); ++i) {

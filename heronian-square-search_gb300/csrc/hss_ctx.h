@@ -46,6 +46,7 @@ struct hss_ctx {
     uint32_t big_cap = 0;
     hss::ExactItem* d_exact = nullptr;    // exact work queue
     uint32_t exact_cap = 0;
+    bool exact_overflow = false;          // the last launch group outgrew it
     uint4* d_merged = nullptr;
     uint32_t merged_cap = 0;
     uint8_t* d_tables = nullptr;
