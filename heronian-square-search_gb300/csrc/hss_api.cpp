@@ -370,18 +370,21 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     LaunchBuffers b = buffers(h, 0);
     std::array<cudaEvent_t, 3> ev;
     if (int e = take_events(h, &ev)) return e;
-    // the group's stream work: items H2D, queue resets, the three kernels
+    // the group's stream work: items H2D, queue resets, the three kernels.
+    // Inside a capture the timing events become event-record nodes
+    // (cudaEventRecordExternal), so they still time the graph's kernels.
+    const unsigned int rec = h->opts.use_graph ? cudaEventRecordExternal : cudaEventRecordDefault;
     auto enqueue = [&]() -> int {
         HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                     h->stream));
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
-        HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
+        HSS_CUDA(h, cudaEventRecordWithFlags(ev[0], h->stream, rec));
         HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
-        HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
+        HSS_CUDA(h, cudaEventRecordWithFlags(ev[1], h->stream, rec));
         HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
         HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
-        HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
+        HSS_CUDA(h, cudaEventRecordWithFlags(ev[2], h->stream, rec));
         return HSS_OK;
     };
     if (h->opts.use_graph) {
