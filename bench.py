@@ -53,8 +53,8 @@ TRAFFIC = ROOT / "profiles" / "traffic.json"
 # parities), each job one row over every STEP-th m; one job per host thread
 # at a time.
 SAMPLE_JOBS = 64
-SAMPLE_STEP = 8          # cpu_baseline of our arm (about 20 s on 16 Arm cores)
-REFERENCE_STEP = 16      # each step of the reference arm (about 10 s)
+SAMPLE_STEP = 4          # cpu_baseline of our arm (about 20 s on 16 Arm cores)
+REFERENCE_STEP = 8       # each step of the reference arm (about 10 s on 16 Arm cores)
 
 # serving stream
 SERVE_SEED = 5
@@ -286,7 +286,8 @@ def our_arm(args, rank, world, local_rank):
         t = json.loads(TRAFFIC.read_text())
         traffic = t.get("batched_kernel_bytes_per_launch")
         if traffic and PEAKS.exists():
-            gbs = traffic / (main_ms * 1e-3) / 1e9
+            groups = max(c["launches"] // 4, 1)  # one persistent launch per launch group
+            gbs = traffic * groups / (main_ms * 1e-3) / 1e9
             peak_gbs = json.loads(PEAKS.read_text()).get("hbm_gbs")
             hbm = {"achieved_gbs": gbs, "peak_gbs": peak_gbs, "frac": gbs / peak_gbs if peak_gbs else None,
                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
