@@ -13,13 +13,13 @@
 //
 // How it is computed here.  The reference multiplies every product out in
 // 128-bit arithmetic.  These kernels decide almost every product from
-//   * residues of the product's coordinates mod 9360, 625 and 119, formed from
+//   * residues of the product's coordinates mod 9360 and 45917, formed from
 //     per-value residues with 32-bit multiplies (exact), and
 //   * float coordinates with a proven error bound: |z| = 2 l^2 m^2 is known per
 //     pair, so every coordinate's float error is below eps = 2 l^2 m^2 2^-20,
 // and only go to exact 128-bit arithmetic when a decision is within eps of a
 // window boundary, or when z passes every residue filter and a fourth root n
-// inside z's float bounds matches z modulo 9360 * 625 * 119 (a possible hit).
+// inside z's float bounds matches z modulo 9360 * 45917 (a possible hit).
 // Counts are therefore exact and every hit is confirmed exactly and rechecked
 // in 256-bit arithmetic.
 //
@@ -38,6 +38,7 @@
 // split prime (gpu_search_v42.cu:318-341).
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
 
 #include "hss_kernels.h"
 
@@ -48,9 +49,8 @@ using u128 = unsigned __int128;
 using i128 = __int128;
 
 constexpr uint32_t kSqA = kModA * kModA;
-constexpr uint32_t kSqB = kModB * kModB;
-constexpr uint32_t kSqC = kModC * kModC;
-constexpr uint32_t kTabA = 0, kTabB = kModA, kTabC = kModA + kModB;
+constexpr uint32_t kSqD = kModD * kModD;
+constexpr uint32_t kTabA = 0, kTabD = kModA;  // byte offsets: field-A bytes, then the field-D bit set
 constexpr uint32_t kSlices = 8;            // plain kernel: blocks per row
 constexpr uint32_t kPlainThreads = 128;    // plain kernel: threads per block
 constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
@@ -68,14 +68,14 @@ struct PairCtx {
     float hi2, hi2o;             // z = S + t counted iff t <= hi2; maybe iff t <= hi2o
     float eps;                   // bound on |float - exact| of a product coordinate
     float sf;                    // S = l^4 + m^4 as float
-    uint32_t sres;               // S mod kModA | mod kModB << 14 | mod kModC << 24 | flag5 << 31
+    uint32_t sres;               // S mod kModA | S mod kModD << 14 | flag5 << 31
     uint32_t dinv;               // inverse of D mod 2^32 (0: pair not on this path)
     uint32_t dthr;               // floor((2^32 - 1) / (8 D))
     uint32_t m;
 };
 
-// Row-side value in shared memory: coordinates as float and their mod-kModA
-// residues (bit 31 of ra: central value); B/C residues kept alongside.
+// Row-side value in shared memory: coordinates as float and their packed
+// residues (fields A and D; bit 31 of ra: central value).
 struct AlphaHot {
     float re, im;
     uint32_t ra, ia;
@@ -87,7 +87,7 @@ struct Acc {
 
 // Event flags per product p (bits 4p .. 4p+3).
 constexpr uint32_t kEvU = 1;   // undecided: count the whole product exactly
-constexpr uint32_t kEvDx = 2;  // orientation (x, y) counted, z passed mod kModA: deep + root filters
+constexpr uint32_t kEvDx = 2;  // orientation (x, y) counted, z passed fields A and D: root filter
 constexpr uint32_t kEvDy = 4;  // the same for orientation (y, x)
 constexpr uint32_t kEvB = 8;   // non-dual pair with both orientations gated: (y, x) still to do
 
@@ -146,6 +146,15 @@ __device__ __forceinline__ bool index_ok(uint32_t i, uint32_t n, unsigned int* e
 __device__ __forceinline__ uint32_t tab_at(const uint8_t* tab, uint32_t base, uint32_t i, uint32_t n,
                                            unsigned int* err) {
     return index_ok(i, n, err) ? tab[base + i] : 0u;
+}
+
+// Bit z of the field-D table: z is a fourth-power residue mod 17, 37 and 73.
+__device__ __forceinline__ uint32_t tab_d(const uint8_t* tab, uint32_t z) {
+    return (reinterpret_cast<const uint32_t*>(tab + kTabD)[z >> 5] >> (z & 31u)) & 1u;
+}
+
+__device__ __forceinline__ uint32_t tab_d_at(const uint8_t* tab, uint32_t z, unsigned int* err) {
+    return index_ok(z, kModD, err) ? tab_d(tab, z) : 0u;
 }
 
 // ----------------------------------------------------------- 256-bit check
@@ -227,10 +236,8 @@ __device__ void exact_test_d(const ExactPair& p, i128 d, i128 area4, uint32_t& c
     u128 z = (u128)sz;
     if (((uint32_t)z & 15u) > 1u) return;
     ++r16;
-    uint32_t rA = mod_u128_small(z, kModA), rB = mod_u128_small(z, kModB);
-    if (!(tab[kTabA + rA] & ((p.flags & 2u) ? 4u : 2u))) return;
-    if ((p.flags & 2u) ? rB != 0 : !tab[kTabB + rB]) return;
-    if (!tab[kTabC + mod_u128_small(z, kModC)]) return;
+    if (!(tab[kTabA + mod_u128_small(z, kModA)] & ((p.flags & 2u) ? 4u : 2u))) return;
+    if (!tab_d(tab, mod_u128_small(z, kModD))) return;
     double zd = (double)(uint64_t)(z >> 64) * 18446744073709551616.0 + (double)(uint64_t)z;
     uint64_t root = (uint64_t)sqrt(sqrt(zd));
     while (root > 0 && (u128)root * root * root * root > z) --root;
@@ -326,13 +333,16 @@ __device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t m) 
 // of the triple (x, y, 2 l^2 m^2).  The non-dual path evaluates the one gated
 // orientation and raises kEvB if both ever pass, so it stays exact regardless.
 template <bool DUAL>
-__device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t bra, uint32_t bia,
+__device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t brw, uint32_t biw,
                                               bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc) {
     const bool ca = (a.ra >> 31) != 0;
-    const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
+    const uint32_t ar = a.ra & kMaskA, ai = a.ia & kMaskA, bra = brw & kMaskA, bia = biw & kMaskA;
+    const uint32_t ad = (a.ra >> kShiftD) & kMaskD, adi = (a.ia >> kShiftD) & kMaskD;
+    const uint32_t bd = (brw >> kShiftD) & kMaskD, bdi = (biw >> kShiftD) & kMaskD;
     const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
+    const uint32_t q1 = ad * bd, q2 = adi * bdi, q3 = ad * bdi, q4 = adi * bd;
     const float f1 = a.re * br, f2 = a.im * bi, f3 = a.re * bi, f4 = a.im * br;
-    const uint32_t sA = c.sres & kMaskA;
+    const uint32_t sA = c.sres & kMaskA, sD = (c.sres >> kShiftD) & kMaskD;
     const uint32_t sel = (c.sres >> 31) ? 4u : 2u;
     uint32_t flags = 0, cnt = 0, r16 = 0;
 #pragma unroll
@@ -340,6 +350,8 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
         const bool valid = p == 0 ? !(ca & cb) : !(ca | cb);
         const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
         const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
+        const uint32_t XD = p ? q1 + q2 : q1 + kSqD - q2;
+        const uint32_t YD = p ? q4 + kSqD - q3 : q3 + q4;
         const float xf = p ? f1 + f2 : f1 - f2;
         const float yf = p ? f4 - f3 : f3 + f4;
         const bool gx = valid & area_gate(Y, c.dinv, c.dthr);  // (D, 4A) = (x, y)
@@ -356,14 +368,20 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             const Window w = window(fabsf(d), c);
             und |= g & w.und;
             const bool ok = g & !w.und;
+            const bool neg = d < 0.f;
             const uint32_t dA = dres % kModA;
-            const uint32_t tA = d < 0.f ? (dA ? kModA - dA : 0u) : dA;
+            const uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
             const uint32_t z1 = sub_mod(sA, tA, kModA), z2 = add_mod(sA, tA, kModA);
             const uint32_t m1 = (ok & w.in1) ? tab[kTabA + z1] : 0u;
             const uint32_t m2 = (ok & w.in2) ? tab[kTabA + z2] : 0u;
             pc += ok ? (uint32_t)w.in1 + (uint32_t)w.in2 : 0u;
             pr += (m1 & 1u) + (m2 & 1u);
-            f |= ((m1 | m2) & sel) ? (oy ? kEvDy : kEvDx) : 0u;
+            // field D of the terms that passed field A
+            const uint32_t dD = (oy ? YD : XD) % kModD;
+            const uint32_t tD = neg ? (dD ? kModD - dD : 0u) : dD;
+            const uint32_t e1 = (m1 & sel) ? tab_d(tab, sub_mod(sD, tD, kModD)) : 0u;
+            const uint32_t e2 = (m2 & sel) ? tab_d(tab, add_mod(sD, tD, kModD)) : 0u;
+            f |= (e1 | e2) ? (oy ? kEvDy : kEvDx) : 0u;
         }
         if (!DUAL) f |= (gx & gy) ? kEvB : 0u;
         // an undecided product is counted whole on the exact path instead
@@ -380,7 +398,7 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
 // A possible hit needs some n in [m, N] with n^4 = z.  From z's float bounds
 // (|error| below sf 2^-22 + eps + |z| 2^-22) take the window of n with n^4
 // inside them, and keep the candidate only if some n of the window has
-// n^4 = z mod 9360, 625 and 119.  The float fourth root sqrtf(sqrtf(x)) is
+// n^4 = z mod 9360 and 45917.  The float fourth root sqrtf(sqrtf(x)) is
 // within 1.5 * 2^-24 relative of x^(1/4) (two correctly rounded square
 // roots), so scaling by 1 -+ 2^-22 (and rounding once more) keeps the bounds
 // on the safe side; 2 units are added on top.  Float and 32-bit integers only.
@@ -397,8 +415,7 @@ __device__ __forceinline__ void root_window(float zf, const PairCtx& c, uint32_t
 
 __device__ __forceinline__ bool root_match(uint32_t n, uint32_t zres) {
     return pow4_mod(n % kModA, kModA) == (zres & kMaskA) &&
-           pow4_mod(n % kModB, kModB) == ((zres >> kShiftB) & kMaskB) &&
-           pow4_mod(n % kModC, kModC) == ((zres >> kShiftC) & kMaskC);
+           pow4_mod(n % kModD, kModD) == ((zres >> kShiftD) & kMaskD);
 }
 
 // One thread scans the window (paths without a warp queue).
@@ -423,21 +440,6 @@ __device__ __forceinline__ bool root_scan_warp(const RootReq& rq, uint32_t lane)
         if (__any_sync(kFull, n <= rq.nhi && root_match(n, rq.zres))) return true;
     }
     return false;
-}
-
-// Residues of the product's coordinates modulo 625 (field 1) or 119
-// (field 2) from the packed value residues.
-__device__ __forceinline__ void coord_res(uint32_t arw, uint32_t aiw, uint32_t brw, uint32_t biw, int field,
-                                          int p, uint32_t& x, uint32_t& y) {
-    const uint32_t shift = field == 1 ? kShiftB : kShiftC;
-    const uint32_t mask = field == 1 ? kMaskB : kMaskC;
-    const uint32_t M = field == 1 ? kModB : kModC;
-    const uint32_t sq = field == 1 ? kSqB : kSqC;
-    uint32_t ar = (arw >> shift) & mask, ai = (aiw >> shift) & mask, br = (brw >> shift) & mask,
-             bi = (biw >> shift) & mask;
-    uint32_t q1 = ar * br, q2 = ai * bi, q3 = ar * bi, q4 = ai * br;
-    x = (p ? q1 + q2 : q1 + sq - q2) % M;
-    y = (p ? q4 + sq - q3 : q3 + q4) % M;
 }
 
 // Exact coordinates for the rare exact path.
@@ -476,107 +478,17 @@ __device__ __forceinline__ void sink_push(const EventSink& s, uint32_t kind) {
     push_exact(*s.buf, kind, s.a, s.b, s.l, s.m, s.row, s.shared_prime != 0);
 }
 
-// Work of one event (one lane), in float and 32-bit integer arithmetic only:
-// an undecided product is queued for exact counting; the (y, x) orientation
-// of a non-dual product whose both orientations passed is decided and
-// counted; every counted orientation whose z passed mod 9360 goes through the
-// mod-625 / mod-119 filters and the fourth-root filter, and survivors are
-// queued for the exact hit test (kind | p << 2 | o << 3).
-//
-// With `slots` (warp-queue paths) the root filter of up to kReqPerLane terms
-// is left to the warp as requests; orientations that the lane itself found
-// possible are returned instead of being queued, so that the caller queues
-// each orientation once.  Returns (candidates, mod-16 survivors, requests
-// left, possible orientations as bits 2p + o).
-__device__ __noinline__ uint4 general_event(uint32_t flags, AlphaHot a, uint32_t arw, uint32_t aiw, HotRec b,
-                                            PairCtx c, uint32_t n_limit, const uint8_t* tab, EventSink sink,
-                                            RootReq* slots) {
-    uint32_t cand = 0, r16 = 0, nreq = 0, passed = 0;
-    const uint32_t ar = a.ra & 0x7FFFFFFFu, ai = a.ia;
-    const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
-    const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
-    const float f1 = a.re * b.re, f2 = a.im * b.im, f3 = a.re * b.im, f4 = a.im * b.re;
-    const uint32_t sA = c.sres & kMaskA, sB = (c.sres >> kShiftB) & kMaskB, sC = (c.sres >> kShiftC) & kMaskC;
-    const bool flag5 = (c.sres >> 31) != 0;
-    const uint32_t sel = flag5 ? 4u : 2u;
-    for (int p = 0; p < 2; ++p) {
-        const uint32_t f = (flags >> (4 * p)) & 15u;
-        if (!f) continue;
-        if (f & kEvU) {
-            sink_push(sink, kExCount | (uint32_t)p << 2);
-            continue;
-        }
-        const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
-        const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
-        const float xf = p ? f1 + f2 : f1 - f2;
-        const float yf = p ? f4 - f3 : f3 + f4;
-        for (int o = 0; o < 2; ++o) {
-            const bool full = o == 1 && (f & kEvB);
-            const bool deep = (f & (o ? kEvDy : kEvDx)) != 0;
-            if (!full && !deep) continue;
-            const float d = o ? yf : xf;
-            const float t = fabsf(d);
-            const Window w = window(t, c);
-            if (full) {
-                if (w.und) {
-                    sink_push(sink, kExOrient | (uint32_t)p << 2 | (uint32_t)o << 3);
-                    continue;
-                }
-                cand += (uint32_t)w.in1 + (uint32_t)w.in2;
-            }
-            const uint32_t dA = (o ? Y : X) % kModA;
-            const bool neg = d < 0.f;
-            const uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
-            const uint32_t zA1 = sub_mod(sA, tA, kModA), zA2 = add_mod(sA, tA, kModA);
-            const uint32_t m1 = w.in1 ? tab_at(tab, kTabA, zA1, kModA, sink.buf->error_flags) : 0u;
-            const uint32_t m2 = w.in2 ? tab_at(tab, kTabA, zA2, kModA, sink.buf->error_flags) : 0u;
-            if (full) r16 += (m1 & 1u) + (m2 & 1u);
-            if (!((m1 | m2) & sel)) continue;
-            uint32_t xB, yB, xC, yC;
-            coord_res(arw, aiw, b.rre, b.rim, 1, p, xB, yB);
-            coord_res(arw, aiw, b.rre, b.rim, 2, p, xC, yC);
-            const uint32_t dB = o ? yB : xB, dC = o ? yC : xC;
-            const uint32_t tB = neg ? (dB ? kModB - dB : 0u) : dB, tC = neg ? (dC ? kModC - dC : 0u) : dC;
-            bool hit_possible = false;
-            for (int term = 0; term < 2 && !hit_possible; ++term) {
-                const uint32_t mm = term ? m2 : m1;
-                if (!(mm & sel)) continue;
-                const uint32_t zB = term ? add_mod(sB, tB, kModB) : sub_mod(sB, tB, kModB);
-                const uint32_t zC = term ? add_mod(sC, tC, kModC) : sub_mod(sC, tC, kModC);
-                if (flag5 ? zB != 0 : !tab_at(tab, kTabB, zB, kModB, sink.buf->error_flags)) continue;
-                if (!tab_at(tab, kTabC, zC, kModC, sink.buf->error_flags)) continue;
-                const float zf = term ? c.sf + t : c.sf - t;
-                uint32_t nlo, nhi;
-                root_window(zf, c, n_limit, nlo, nhi);
-                const uint32_t zres = (term ? zA2 : zA1) | (zB << kShiftB) | (zC << kShiftC);
-                if (slots && nreq < kReqPerLane)
-                    slots[nreq++] = RootReq{nlo, nhi, zres, 2u * (uint32_t)p + (uint32_t)o};
-                else if (root_scan(nlo, nhi, zres))
-                    hit_possible = true;
-            }
-            if (hit_possible) {
-                if (slots)
-                    passed |= 1u << (2 * p + o);
-                else
-                    sink_push(sink, kExHit | (uint32_t)p << 2 | (uint32_t)o << 3);
-            }
-        }
-    }
-    return make_uint4(cand, r16, nreq, passed);
-}
-
-// One deep unit of an event: orientation o of product p (p = 1: alpha *
-// conj(beta)) was counted by the filter loop and its z passed the mod-kModA
-// table for some term.  The coordinate D of the orientation is
-// u + v, u - v or v - u with u, v = (ar br, ai bi) for o = 0 and
-// (ar bi, ai br) for o = 1; everything is computed branch-free in p and o, so
-// lanes holding different units run one instruction stream.  Terms that pass
-// the mod-625 and mod-119 tables go to the root filter: left as requests in
-// `slots` while there is room, else scanned here; returns true when such a
-// scan found a possible root.
-__device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot& a, uint32_t arw, uint32_t aiw,
-                                          const HotRec& b, const PairCtx& c, uint32_t n_limit, const uint8_t* tab,
-                                          RootReq* slots, uint32_t& nreq, unsigned int* err) {
+// One counted orientation o of product p (p = 1: alpha * conj(beta)) through
+// the residue filters.  The coordinate D of the orientation is u + v, u - v
+// or v - u with u, v = (ar br, ai bi) for o = 0 and (ar bi, ai br) for o = 1;
+// both residue fields are computed branch-free in p and o, so lanes holding
+// different orientations run one instruction stream.  Counted terms whose z
+// passes the field-A and field-D tables go to the root filter: left as
+// requests in `slots` while there is room, else scanned here; returns true
+// when such a scan found a possible root.
+__device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot& a, const HotRec& b,
+                                          const PairCtx& c, uint32_t n_limit, const uint8_t* tab, RootReq* slots,
+                                          uint32_t& nreq, unsigned int* err) {
     const bool plus = o != p;
     const float fu = o ? a.re * b.im : a.re * b.re;
     const float fv = o ? a.im * b.re : a.im * b.im;
@@ -584,34 +496,28 @@ __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot
     const float t = fabsf(d);
     const bool neg = d < 0.f;
     // D mod M from the packed residues of one field, signed by d
-    auto field = [&](uint32_t wa, uint32_t wai, uint32_t wb, uint32_t wbi, uint32_t M) {
+    auto field = [&](uint32_t shift, uint32_t mask, uint32_t M) {
+        const uint32_t wa = (a.ra >> shift) & mask, wai = (a.ia >> shift) & mask;
+        const uint32_t wb = (b.rre >> shift) & mask, wbi = (b.rim >> shift) & mask;
         const uint32_t u = o ? wa * wbi : wa * wb, v = o ? wai * wb : wai * wbi;
         const uint32_t r = (plus ? u + v : (o ? v + M * M - u : u + M * M - v)) % M;
         return neg ? (r ? M - r : 0u) : r;
     };
-    const uint32_t tA = field(a.ra & 0x7FFFFFFFu, a.ia, b.rre & kMaskA, b.rim & kMaskA, kModA);
+    const uint32_t tA = field(0u, kMaskA, kModA), tD = field(kShiftD, kMaskD, kModD);
     const Window w = window(t, c);
-    const uint32_t sA = c.sres & kMaskA, sB = (c.sres >> kShiftB) & kMaskB, sC = (c.sres >> kShiftC) & kMaskC;
-    const bool flag5 = (c.sres >> 31) != 0;
-    const uint32_t sel = flag5 ? 4u : 2u;
-    const uint32_t zA1 = sub_mod(sA, tA, kModA), zA2 = add_mod(sA, tA, kModA);
-    const uint32_t m1 = w.in1 ? tab_at(tab, kTabA, zA1, kModA, err) : 0u;
-    const uint32_t m2 = w.in2 ? tab_at(tab, kTabA, zA2, kModA, err) : 0u;
-    const uint32_t tB = field((arw >> kShiftB) & kMaskB, (aiw >> kShiftB) & kMaskB, (b.rre >> kShiftB) & kMaskB,
-                              (b.rim >> kShiftB) & kMaskB, kModB);
-    const uint32_t tC = field((arw >> kShiftC) & kMaskC, (aiw >> kShiftC) & kMaskC, (b.rre >> kShiftC) & kMaskC,
-                              (b.rim >> kShiftC) & kMaskC, kModC);
+    const uint32_t sA = c.sres & kMaskA, sD = (c.sres >> kShiftD) & kMaskD;
+    const uint32_t sel = (c.sres >> 31) ? 4u : 2u;
     bool hit = false;
 #pragma unroll
     for (int term = 0; term < 2; ++term) {
-        if (!((term ? m2 : m1) & sel)) continue;
-        const uint32_t zB = term ? add_mod(sB, tB, kModB) : sub_mod(sB, tB, kModB);
-        const uint32_t zC = term ? add_mod(sC, tC, kModC) : sub_mod(sC, tC, kModC);
-        if (flag5 ? zB != 0 : !tab_at(tab, kTabB, zB, kModB, err)) continue;
-        if (!tab_at(tab, kTabC, zC, kModC, err)) continue;
+        if (!(term ? w.in2 : w.in1)) continue;
+        const uint32_t zA = term ? add_mod(sA, tA, kModA) : sub_mod(sA, tA, kModA);
+        if (!(tab_at(tab, kTabA, zA, kModA, err) & sel)) continue;
+        const uint32_t zD = term ? add_mod(sD, tD, kModD) : sub_mod(sD, tD, kModD);
+        if (!tab_d_at(tab, zD, err)) continue;
         uint32_t nlo, nhi;
         root_window(term ? c.sf + t : c.sf - t, c, n_limit, nlo, nhi);
-        const uint32_t zres = (term ? zA2 : zA1) | (zB << kShiftB) | (zC << kShiftC);
+        const uint32_t zres = zA | (zD << kShiftD);
         if (slots && nreq < kReqPerLane)
             slots[nreq++] = RootReq{nlo, nhi, zres, 2u * p + o};
         else if (!hit && root_scan(nlo, nhi, zres))
@@ -620,22 +526,83 @@ __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot
     return hit;
 }
 
+// Work of one event (one lane) that holds an undecided product or a
+// non-dual product whose both orientations passed, in float and 32-bit
+// integer arithmetic only: an undecided product is queued for exact
+// counting; the (y, x) orientation of the second kind is decided and counted
+// (or queued for exact counting when undecided); every counted orientation
+// that is marked, or that was just counted, goes through deep_unit, and
+// possible hits are queued for the exact test (kind | p << 2 | o << 3).
+//
+// With `slots` (warp-queue paths) the root filter of up to kReqPerLane terms
+// is left to the warp as requests; orientations that the lane itself found
+// possible are returned instead of being queued, so that the caller queues
+// each orientation once.  Returns (candidates, mod-16 survivors, requests
+// left, possible orientations as bits 2p + o).
+__device__ __noinline__ uint4 general_event(uint32_t flags, AlphaHot a, HotRec b, PairCtx c, uint32_t n_limit,
+                                            const uint8_t* tab, EventSink sink, RootReq* slots) {
+    uint32_t cand = 0, r16 = 0, nreq = 0, passed = 0;
+    const uint32_t ar = a.ra & kMaskA, ai = a.ia & kMaskA;
+    const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
+    const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
+    const float f1 = a.re * b.re, f2 = a.im * b.im, f3 = a.re * b.im, f4 = a.im * b.re;
+    const uint32_t sA = c.sres & kMaskA;
+    unsigned int* err = sink.buf->error_flags;
+    for (uint32_t p = 0; p < 2; ++p) {
+        const uint32_t f = (flags >> (4 * p)) & 15u;
+        if (!f) continue;
+        if (f & kEvU) {
+            sink_push(sink, kExCount | p << 2);
+            continue;
+        }
+        const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
+        const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
+        const float xf = p ? f1 + f2 : f1 - f2;
+        const float yf = p ? f4 - f3 : f3 + f4;
+        for (uint32_t o = 0; o < 2; ++o) {
+            const bool full = o == 1 && (f & kEvB);
+            const bool deep = (f & (o ? kEvDy : kEvDx)) != 0;
+            if (!full && !deep) continue;
+            if (full) {
+                const float d = o ? yf : xf;
+                const Window w = window(fabsf(d), c);
+                if (w.und) {
+                    sink_push(sink, kExOrient | p << 2 | o << 3);
+                    continue;
+                }
+                cand += (uint32_t)w.in1 + (uint32_t)w.in2;
+                const uint32_t dA = (o ? Y : X) % kModA;
+                const uint32_t tA = d < 0.f ? (dA ? kModA - dA : 0u) : dA;
+                if (w.in1) r16 += tab_at(tab, kTabA, sub_mod(sA, tA, kModA), kModA, err) & 1u;
+                if (w.in2) r16 += tab_at(tab, kTabA, add_mod(sA, tA, kModA), kModA, err) & 1u;
+            }
+            if (deep_unit(p, o, a, b, c, n_limit, tab, slots, nreq, err)) {
+                if (slots)
+                    passed |= 1u << (2 * p + o);
+                else
+                    sink_push(sink, kExHit | p << 2 | o << 3);
+            }
+        }
+    }
+    return make_uint4(cand, r16, nreq, passed);
+}
+
 // Work of one event: events with an undecided product or a non-dual product
 // whose both orientations passed take the general path; the others are a set
-// of deep units (one bit per counted orientation whose z passed mod kModA).
-// Returns (candidates, mod-16 survivors, requests left, possible
+// of deep units (one bit per counted orientation whose z passed fields A and
+// D).  Returns (candidates, mod-16 survivors, requests left, possible
 // orientations) as general_event does.
-__device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a, uint32_t arw, uint32_t aiw,
-                                               const HotRec& b, const PairCtx& c, uint32_t n_limit,
-                                               const uint8_t* tab, const EventSink& sink, RootReq* slots) {
-    if (flags & ((kEvU | kEvB) * 0x11u)) return general_event(flags, a, arw, aiw, b, c, n_limit, tab, sink, slots);
+__device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a, const HotRec& b, const PairCtx& c,
+                                               uint32_t n_limit, const uint8_t* tab, const EventSink& sink,
+                                               RootReq* slots) {
+    if (flags & ((kEvU | kEvB) * 0x11u)) return general_event(flags, a, b, c, n_limit, tab, sink, slots);
     uint32_t units = ((flags & kEvDx) ? 1u : 0u) | ((flags & kEvDy) ? 2u : 0u) |
                      ((flags & (kEvDx << 4)) ? 4u : 0u) | ((flags & (kEvDy << 4)) ? 8u : 0u);
     uint32_t nreq = 0, passed = 0;
     while (units) {
         const uint32_t u = __ffs(units) - 1;
         units &= units - 1;
-        if (deep_unit(u >> 1, u & 1u, a, arw, aiw, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags)) {
+        if (deep_unit(u >> 1, u & 1u, a, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags)) {
             if (slots)
                 passed |= 1u << u;
             else
@@ -651,11 +618,11 @@ __device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a
 // instruction cache; it has no 128-bit code, so the call costs few registers.
 // With `slots`, x also carries the root requests left (bits 16-19) and the
 // orientations already found possible (bits 20-23).
-__device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, uint2 abc, HotRec b, PairCtx c, uint32_t ka,
-                                              uint32_t j, uint32_t l, uint32_t row, const uint8_t* tab,
-                                              uint32_t limit, const LaunchBuffers* buf, RootReq* slots = nullptr) {
+__device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, HotRec b, PairCtx c, uint32_t ka, uint32_t j,
+                                              uint32_t l, uint32_t row, const uint8_t* tab, uint32_t limit,
+                                              const LaunchBuffers* buf, RootReq* slots = nullptr) {
     const EventSink sink{buf, ka, j, l, pair_m(c), row, 0u};
-    const uint4 r = process_event(flags, a, abc.x, abc.y, b, c, limit, tab, sink, slots);
+    const uint4 r = process_event(flags, a, b, c, limit, tab, sink, slots);
     return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
 
@@ -734,11 +701,10 @@ __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uin
     uint32_t D = 3u * (f3 ? 3u : 1u) * (f5 ? 5u : 1u);
     c.dinv = inverse_odd(D);
     c.dthr = 0xFFFFFFFFu / (8u * D);
-    uint32_t mA = (uint32_t)(m % kModA), mB = (uint32_t)(m % kModB), mC = (uint32_t)(m % kModC);
+    uint32_t mA = (uint32_t)(m % kModA), mD = (uint32_t)(m % kModD);
     uint32_t sA = (R.lmodA + pow4_mod(mA, kModA)) % kModA;
-    uint32_t sB = (R.lmodB + pow4_mod(mB, kModB)) % kModB;
-    uint32_t sC = (R.lmodC + pow4_mod(mC, kModC)) % kModC;
-    c.sres = sA | (sB << kShiftB) | (sC << kShiftC) | (f5 ? 0x80000000u : 0u);
+    uint32_t sD = (R.lmodD + pow4_mod(mD, kModD)) % kModD;
+    c.sres = sA | (sD << kShiftD) | (f5 ? 0x80000000u : 0u);
     uint32_t areaA = 2u * (R.l2modA * (uint32_t)(m2 % kModA) % kModA);
     bool cc = area_gate(areaA, c.dinv, c.dthr) && w <= 0;
     cc_cand = cc ? 1u : 0u;
@@ -748,22 +714,20 @@ __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uin
 
 // Row value alpha scaled by 2 (the factor 2 of 2 l^2 m^2; the reference
 // doubles the product instead, gpu_search_v42.cu:223-225).
-__device__ __forceinline__ void scale2(const HotRec& h, AlphaHot& a, uint2& abc) {
+__device__ __forceinline__ void scale2(const HotRec& h, AlphaHot& a) {
     a.re = 2.f * h.re;
     a.im = 2.f * h.im;
     uint32_t w[2] = {h.rre, h.rim};
     uint32_t out[2];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-        uint32_t ra = w[i] & kMaskA, rb = (w[i] >> kShiftB) & kMaskB, rc = (w[i] >> kShiftC) & kMaskC;
+        uint32_t ra = w[i] & kMaskA, rd = (w[i] >> kShiftD) & kMaskD;
         ra = 2 * ra >= kModA ? 2 * ra - kModA : 2 * ra;
-        rb = 2 * rb >= kModB ? 2 * rb - kModB : 2 * rb;
-        rc = 2 * rc >= kModC ? 2 * rc - kModC : 2 * rc;
-        out[i] = ra | (rb << kShiftB) | (rc << kShiftC);
+        rd = 2 * rd >= kModD ? 2 * rd - kModD : 2 * rd;
+        out[i] = ra | (rd << kShiftD);
     }
-    a.ra = (out[0] & kMaskA) | (h.rre & kCentralBit);
-    a.ia = out[1] & kMaskA;
-    abc = make_uint2(out[0], out[1]);
+    a.ra = out[0] | (h.rre & kCentralBit);
+    a.ia = out[1];
 }
 
 __device__ __forceinline__ void push_merged(const LaunchBuffers& buf, uint32_t l, uint32_t m, uint32_t row) {
@@ -881,7 +845,7 @@ __device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t slot
 // consecutive records are consecutive in memory) is found by a binary search
 // over the lanes' inclusive prefix sums, then within the owner lane.
 template <bool DUAL>
-__device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint2* s_abc, uint32_t na,
+__device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t na,
                                              const PairCtx* wctx, const uint32_t (&cnt)[kRootsPerLane],
                                              const uint32_t (&s0)[kRootsPerLane], uint32_t lane,
                                              const DeviceCache& cache, const uint8_t* s_tab, uint32_t a0, uint64_t l,
@@ -902,7 +866,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
     auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
         if (!index_ok(k, na, buf.error_flags) || !index_ok(slot, 32 * kRootsPerLane, buf.error_flags)) return 0u;
-        const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], s_abc[k], cache.hot[j], wctx[slot], a0 + k, j,
+        const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], cache.hot[j], wctx[slot], a0 + k, j,
                                      (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
         acc.cand += r.x & 0xFFFFu;
         acc.r16 += r.y;
@@ -937,12 +901,11 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, const uint
         const bool live = r < total;
         const PairCtx c = wctx[slot];
         const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
-        const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
         const bool cb = (b.rre & kCentralBit) != 0;
         for (uint32_t k = 0; k < na; ++k) {
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
-            if (live) flags = eval_fast<DUAL>(a, b.re, b.im, bra, bia, cb, c, s_tab, acc);
+            if (live) flags = eval_fast<DUAL>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
             if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
@@ -957,8 +920,7 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
     constexpr uint32_t kChunk = 32 * kRootsPerLane;
     extern __shared__ __align__(16) unsigned char smem[];
     AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
-    uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
-    PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_abc + alpha_cap);
+    PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_alpha + alpha_cap);
     uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * kChunk);
     RootReq* s_req = reinterpret_cast<RootReq*>(s_queue + kWarps * kQueue);
     uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kWarps * 32 * kReqPerLane);
@@ -983,7 +945,7 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
         const WorkItem w = items[it];
         const RowInfo& R = buf.row_info[w.row];
         const uint32_t a0 = R.seg, na = R.free_l + 1;
-        for (uint32_t i = tid; i < na; i += NT) scale2(cache.hot[a0 + i], s_alpha[i], s_abc[i]);
+        for (uint32_t i = tid; i < na; i += NT) scale2(cache.hot[a0 + i], s_alpha[i]);
         __syncthreads();
         const uint32_t nm = w.m1 - w.m0;
         for (;;) {
@@ -1022,10 +984,10 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
                 }
             }
             __syncwarp();
-            batched_pass<false>(s_alpha, s_abc, na, wctx, cnt_single, s0, lane, cache, s_tab, a0, w.l, w.row, buf,
+            batched_pass<false>(s_alpha, na, wctx, cnt_single, s0, lane, cache, s_tab, a0, w.l, w.row, buf,
                                 q, qn, wreq, acc);
             if (__any_sync(kFull, any_dual))
-                batched_pass<true>(s_alpha, s_abc, na, wctx, cnt_dual, s0, lane, cache, s_tab, a0, w.l, w.row, buf, q,
+                batched_pass<true>(s_alpha, na, wctx, cnt_dual, s0, lane, cache, s_tab, a0, w.l, w.row, buf, q,
                                    qn, wreq, acc);
             __syncwarp();
         }
@@ -1041,14 +1003,13 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
                                                                  const LaunchBuffers buf) {
     extern __shared__ __align__(16) unsigned char smem[];
     AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
-    uint2* s_abc = reinterpret_cast<uint2*>(s_alpha + alpha_cap);
-    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_abc + alpha_cap);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_alpha + alpha_cap);
     const uint32_t row = blockIdx.x / kSlices, slice = blockIdx.x % kSlices;
     const RowInfo& R = buf.row_info[row];
     const uint64_t l = R.l;
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kPlainThreads) s_tab[i] = buf.tables[i];
     const uint32_t a0 = R.seg, na = R.free_l + 1;
-    for (uint32_t i = threadIdx.x; i < na; i += kPlainThreads) scale2(cache.hot[a0 + i], s_alpha[i], s_abc[i]);
+    for (uint32_t i = threadIdx.x; i < na; i += kPlainThreads) scale2(cache.hot[a0 + i], s_alpha[i]);
     __syncthreads();
     Acc acc{0, 0, 0, 0, 0, 0};
     const uint64_t n = cache.limit;
@@ -1069,13 +1030,13 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
         acc.r16 += cc_r;
         for (uint32_t j = s0; j < s1; ++j) {
             const HotRec b = cache.hot[j];
-            const uint32_t bra = b.rre & kMaskA, bia = b.rim & kMaskA;
             const bool cb = (b.rre & kCentralBit) != 0;
             for (uint32_t k = 0; k < na; ++k) {
-                const uint32_t flags = pair_dual(c) ? eval_fast<true>(s_alpha[k], b.re, b.im, bra, bia, cb, c, s_tab, acc)
-                                                    : eval_fast<false>(s_alpha[k], b.re, b.im, bra, bia, cb, c, s_tab, acc);
+                const uint32_t flags =
+                    pair_dual(c) ? eval_fast<true>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc)
+                                 : eval_fast<false>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
                 if (flags)
-                    add_event(acc, cached_event(flags, s_alpha[k], s_abc[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab,
+                    add_event(acc, cached_event(flags, s_alpha[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab,
                                                 (uint32_t)n, &buf));
             }
         }
@@ -1153,15 +1114,15 @@ __device__ void group_value(const DeviceCache& cache, const Group& g, uint32_t k
     im = xi;
 }
 
-// Complex product of packed residues (mod 9360 | 625 << 14 | 119 << 24).
+// Complex product of packed residues (fields A and D).
 __device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, uint32_t bi, uint32_t& xr,
                                         uint32_t& xi) {
     uint32_t outr = 0, outi = 0;
 #pragma unroll
-    for (int f = 0; f < 3; ++f) {
-        const uint32_t shift = f == 0 ? 0u : (f == 1 ? kShiftB : kShiftC);
-        const uint32_t mask = f == 0 ? kMaskA : (f == 1 ? kMaskB : kMaskC);
-        const uint32_t M = f == 0 ? kModA : (f == 1 ? kModB : kModC);
+    for (int f = 0; f < 2; ++f) {
+        const uint32_t shift = f == 0 ? 0u : kShiftD;
+        const uint32_t mask = f == 0 ? kMaskA : kMaskD;
+        const uint32_t M = f == 0 ? kModA : kModD;
         const uint32_t a0 = (ar >> shift) & mask, a1 = (ai >> shift) & mask;
         const uint32_t b0 = (br >> shift) & mask, b1 = (bi >> shift) & mask;
         outr |= ((a0 * b0 + M * M - a1 * b1) % M) << shift;
@@ -1173,7 +1134,7 @@ __device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, u
 
 // List entry k of group g multiplied out in float and residues (the same
 // decode as group_value; the exact value is rebuilt only for exact work).
-__device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32_t k, AlphaHot& out, uint2& abc) {
+__device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32_t k, AlphaHot& out) {
     float xr = g.scale_f, xi = 0.f;
     uint32_t rr = g.scale_res, ri = 0u;
     uint32_t i = 0;
@@ -1189,7 +1150,7 @@ __device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32
     auto mul = [&](const HotRec& v) {
         const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
         uint32_t yr, yi;
-        res_mul(rr, ri, v.rre & 0x7FFFFFFFu, v.rim, yr, yi);
+        res_mul(rr, ri, v.rre & kResMask, v.rim, yr, yi);
         xr = nr;
         xi = ni;
         rr = yr;
@@ -1210,28 +1171,17 @@ __device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32
     }
     out.re = xr;
     out.im = xi;
-    out.ra = (rr & kMaskA) | (central ? kCentralBit : 0u);
-    out.ia = ri & kMaskA;
-    abc = make_uint2(rr, ri);
-}
-
-__device__ void list_entry(i128 re, i128 im, bool central, AlphaHot& a, uint2& abc) {
-    uint32_t rw = pack_residues(re), iw = pack_residues(im);
-    a.re = i128_to_float(re);
-    a.im = i128_to_float(im);
-    a.ra = (rw & kMaskA) | (central ? kCentralBit : 0u);
-    a.ia = iw & kMaskA;
-    abc = make_uint2(rw, iw);
+    out.ra = rr | (central ? kCentralBit : 0u);
+    out.ia = ri;
 }
 
 // One event of a shared-prime pair: list entries ka (alpha side) and kb.
-__device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, uint2 abc, AlphaHot bh, uint2 bbc,
-                                              PairCtx c, uint32_t ka, uint32_t kb, uint32_t l, uint32_t row,
-                                              const uint8_t* tab, uint32_t limit, const LaunchBuffers* buf,
-                                              RootReq* slots = nullptr) {
-    const HotRec b{bh.re, bh.im, bbc.x | (bh.ra & kCentralBit), bbc.y};
+__device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, AlphaHot bh, PairCtx c, uint32_t ka,
+                                              uint32_t kb, uint32_t l, uint32_t row, const uint8_t* tab,
+                                              uint32_t limit, const LaunchBuffers* buf, RootReq* slots = nullptr) {
+    const HotRec b{bh.re, bh.im, bh.ra, bh.ia};
     const EventSink sink{buf, ka, kb, l, pair_m(c), row, 1u};
-    const uint4 r = process_event(flags, a, abc.x, abc.y, b, c, limit, tab, sink, slots);
+    const uint4 r = process_event(flags, a, b, c, limit, tab, sink, slots);
     return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
 
@@ -1350,8 +1300,7 @@ __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint
 
 // Entry k of side g of a described pair, in float and residues (the decode
 // of group_value, with the block sizes recomputed from the exponents).
-__device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int g, uint32_t k, AlphaHot& out,
-                               uint2& abc) {
+__device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int g, uint32_t k, AlphaHot& out) {
     const uint32_t count = D.count[g];
     uint32_t suffix[kDescTerms];
     for (int i = (int)count - 1, acc = 1; i >= 0; --i) {
@@ -1363,7 +1312,7 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
     auto mul = [&](const HotRec& v) {
         const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
         uint32_t yr, yi;
-        res_mul(rr, ri, v.rre & 0x7FFFFFFFu, v.rim, yr, yi);
+        res_mul(rr, ri, v.rre & kResMask, v.rim, yr, yi);
         xr = nr;
         xi = ni;
         rr = yr;
@@ -1393,9 +1342,8 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
     }
     out.re = xr;
     out.im = xi;
-    out.ra = (rr & kMaskA) | (central ? kCentralBit : 0u);
-    out.ia = ri & kMaskA;
-    abc = make_uint2(rr, ri);
+    out.ra = rr | (central ? kCentralBit : 0u);
+    out.ia = ri;
 }
 
 // Shared-prime pairs, a warp per pair, 32 pairs set up at once: each lane
@@ -1409,7 +1357,6 @@ constexpr uint32_t kPairWarps = 4;
 __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
     __shared__ PairDesc s_desc[kPairWarps][32];
     __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
-    __shared__ uint2 s_lbc[kPairWarps][kWarpListCap];
     __shared__ uint64_t s_queue[kPairWarps][kQueue];
     // dynamic (static use is near 48 KB): root requests, then the tables
     extern __shared__ __align__(16) unsigned char s_dyn[];
@@ -1420,7 +1367,6 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
     PairDesc* desc = s_desc[warp];
     AlphaHot* list = s_list[warp];
-    uint2* lbc = s_lbc[warp];
     uint64_t* q = s_queue[warp];
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
@@ -1461,7 +1407,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1;
             for (uint32_t k = lane; k < na + nb; k += 32) {
                 const int side = k < na ? 0 : 1;
-                desc_value_hot(cache, D, side, side ? k - na : k, list[k], lbc[k]);
+                desc_value_hot(cache, D, side, side ? k - na : k, list[k]);
             }
             __syncwarp();
             const PairCtx c = D.ctx;
@@ -1471,8 +1417,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
                 if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
-                const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], lbc[ka], list[na + kb], lbc[na + kb], c,
-                                             ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
+                const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], list[na + kb], c, ka, kb, l, row, s_tab,
+                                             (uint32_t)cache.limit, &buf, slots);
                 acc.cand += r.x & 0xFFFFu;
                 acc.r16 += r.y;
                 return r.x >> 16;
@@ -1498,9 +1444,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                         kb -= (int32_t)nb;
                     }
                     const AlphaHot a = list[ka], bh = list[na + kb];
-                    flags = dual ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
+                    flags = dual ? eval_fast<true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0,
                                                    c, s_tab, acc)
-                                 : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0,
+                                 : eval_fast<false>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0,
                                                     c, s_tab, acc);
                 }
                 if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags)))
@@ -1519,8 +1465,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
 __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
     __shared__ MergedShared S;
     __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
-    __shared__ uint2 s_lbc[kMergedListCap];
-    __shared__ uint8_t s_tab[kTableBytes];
+    __shared__ __align__(16) uint8_t s_tab[kTableBytes];
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
     const uint32_t count = min(*buf.big_count, buf.big_cap);
     for (uint32_t qi = blockIdx.x; qi < count; qi += gridDim.x) {
@@ -1541,7 +1486,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         for (uint32_t k = threadIdx.x; k < na + nb; k += kMergedThreads) {
             const int side = k < na ? 0 : 1;
             const uint32_t idx = side ? k - na : k;
-            group_value_hot(cache, S.g[side], idx, s_list[k], s_lbc[k]);
+            group_value_hot(cache, S.g[side], idx, s_list[k]);
         }
         __syncthreads();
         Acc acc{0, 0, 0, 0, 0, 0};
@@ -1556,12 +1501,12 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
             const uint32_t ka = k / nb, kb = k - ka * nb;
             const AlphaHot a = s_list[ka], bh = s_list[na + kb];
             const uint32_t flags =
-                pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
-                             : eval_fast<false>(a, bh.re, bh.im, bh.ra & 0x7FFFFFFFu, bh.ia, (bh.ra >> 31) != 0, c, s_tab,
+                pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
+                             : eval_fast<false>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab,
                                                 acc);
             if (flags)
-                add_event(acc, merged_event(flags, a, s_lbc[ka], bh, s_lbc[na + kb], c, ka, kb, (uint32_t)S.l, S.row,
-                                            s_tab, (uint32_t)cache.limit, &buf));
+                add_event(acc, merged_event(flags, a, bh, c, ka, kb, (uint32_t)S.l, S.row, s_tab,
+                                            (uint32_t)cache.limit, &buf));
         }
         flush_acc(acc, &buf.rows[S.row], true);
     }
@@ -1572,7 +1517,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
 // coordinates come from the cache (row values doubled) or, for pairs that
 // share a split prime, from the two term groups rebuilt for the pair.
 __global__ void __launch_bounds__(128) exact_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ uint8_t s_tab[kTableBytes];
+    __shared__ __align__(16) uint8_t s_tab[kTableBytes];
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += blockDim.x) s_tab[i] = buf.tables[i];
     __syncthreads();
     const uint32_t count = min(*buf.exact_count, buf.exact_cap);
@@ -1665,8 +1610,8 @@ void fill_row_info(const uint32_t* spf, const uint32_t* seg_off, uint64_t n, uin
     R->l4 = (u128)R->l2 * R->l2;
     R->n4 = (u128)(n * n) * (n * n);
     R->lmodA = mod_u128_small(R->l4, kModA);
-    R->lmodB = mod_u128_small(R->l4, kModB);
-    R->lmodC = mod_u128_small(R->l4, kModC);
+    R->lmodD = mod_u128_small(R->l4, kModD);
+    R->spare = 0;
     R->l2modA = (uint32_t)(R->l2 % kModA);
     R->l3 = l % 3 == 0;
     R->l5 = l % 5 == 0;
@@ -1709,13 +1654,19 @@ void build_residue_tables(uint8_t* out) {
         out[kTabA + z] = (uint8_t)((m16 ? 1u : 0u) | ((m16 && m9 && m5) ? 2u : 0u) |
                                    ((m16 && m9 && z % 5 == 0) ? 4u : 0u));
     }
-    for (uint32_t z = 0; z < kModB; ++z) out[kTabB + z] = is4(z, kModB) ? 1 : 0;
-    for (uint32_t z = 0; z < kModC; ++z) out[kTabC + z] = (is4(z % 7, 7) && is4(z % 17, 17)) ? 1 : 0;
+    bool r17[17], r37[37], r73[73];
+    for (uint32_t z = 0; z < 17; ++z) r17[z] = is4(z, 17);
+    for (uint32_t z = 0; z < 37; ++z) r37[z] = is4(z, 37);
+    for (uint32_t z = 0; z < 73; ++z) r73[z] = is4(z, 73);
+    uint32_t words[kTabDWords] = {};
+    for (uint32_t z = 0; z < kModD; ++z)
+        if (r17[z % 17] && r37[z % 37] && r73[z % 73]) words[z >> 5] |= 1u << (z & 31u);
+    memcpy(out + kTabD, words, sizeof words);
 }
 
 size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
     const uint32_t warps = (uint32_t)threads / 32;
-    return (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) +
+    return (size_t)alpha_cap * sizeof(AlphaHot) +
            (size_t)warps * 32 * kRootsPerLane * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
            (size_t)warps * 32 * kReqPerLane * sizeof(RootReq) + kTableBytes;
 }
@@ -1749,7 +1700,7 @@ cudaError_t launch_batched(const DeviceCache& cache, const WorkItem* items, uint
 cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_rows, uint32_t alpha_cap,
                          const LaunchBuffers& buf, cudaStream_t stream) {
     (void)first_l;
-    size_t smem = (size_t)alpha_cap * (sizeof(AlphaHot) + sizeof(uint2)) + kTableBytes;
+    size_t smem = (size_t)alpha_cap * sizeof(AlphaHot) + kTableBytes;
     cudaError_t e = cudaFuncSetAttribute((const void*)plain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;

@@ -7,14 +7,17 @@
 
 namespace hss {
 
-// Sizes of the residue tables the kernels stage in shared memory:
-// tabA[z mod 9360] bit0: z mod 16 in {0,1}; bit1: bit0 and z mod 9, 5 and 13
-// fourth-power residues; bit2: bit0, z mod 9 and 13 residues and 5 | z.
-// tabB[z mod 625]: fourth-power residue mod 625.  tabC[z mod 119]:
-// fourth-power residue mod 7 and 17.  Together they hold the conditions of
-// the reference's mod 16, 9, 5, 625 and 7*13*17 tables
-// (gpu_search_v42.cu:166-170), regrouped by modulus.
-constexpr uint32_t kTableBytes = kModA + kModB + kModC;
+// Residue tables the kernels stage in shared memory:
+// tabA[z mod 9360] (bytes) bit0: z mod 16 in {0,1}; bit1: bit0 and z mod 9,
+// 5 and 13 fourth-power residues; bit2: bit0, z mod 9 and 13 residues and
+// 5 | z.  tabD (bit set from byte kModA, 32-bit words): bit z mod 45917 set
+// when z is a fourth-power residue mod 17, 37 and 73.  These are necessary
+// conditions for z = n^4, like the reference's mod 16, 9, 5, 625 and 7*13*17
+// tables (gpu_search_v42.cu:166-170); the moduli are chosen for filtering
+// power per bit (the exact test decides every hit).
+constexpr uint32_t kTabDWords = (kModD + 31) / 32;
+constexpr uint32_t kTableBytes = kModA + 4 * kTabDWords;
+static_assert(kModA % 4 == 0, "the bit set starts on a word");
 void build_residue_tables(uint8_t* out /* kTableBytes */);
 
 // Constants of one root row, built on the host for every row of a launch
@@ -25,7 +28,7 @@ struct RowInfo {
     uint64_t l, l2;
     unsigned __int128 l4, n4;
     uint64_t fixed;             // prod of non-split p^(2a) of l
-    uint32_t lmodA, lmodB, lmodC, l2modA;  // l^4 mod kModA, kModB, kModC; l^2 mod kModA
+    uint32_t lmodA, lmodD, l2modA, spare;  // l^4 mod kModA, kModD; l^2 mod kModA
     uint32_t l3, l5, leven, nodd;          // 3 | l, 5 | l, l even, number of odd primes
     uint32_t pinv[9], pthr[9];
     uint32_t psplit;            // bit i set when odd prime i is = 1 mod 4

@@ -33,7 +33,7 @@ inline uint32_t residue64(int64_t v, uint32_t m) {
 }
 
 inline uint32_t pack64(int64_t v) {
-    return residue64(v, kModA) | (residue64(v, kModB) << kShiftB) | (residue64(v, kModC) << kShiftC);
+    return residue64(v, kModA) | (residue64(v, kModD) << kShiftD);
 }
 
 inline HotRec make_hot(int64_t re, int64_t im, bool central) {
