@@ -332,9 +332,13 @@ __device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t m) 
 // = 0 mod 8; if 3 (or 5) does not divide 2 l^2 m^2 it divides at most one leg
 // of the triple (x, y, 2 l^2 m^2).  The non-dual path evaluates the one gated
 // orientation and raises kEvB if both ever pass, so it stays exact regardless.
-template <bool DUAL>
+// MODE 0: non-dual pair, 1: dual pair, 2: either (dual_rt), one code copy for
+// kernels whose lanes meet both kinds and whose instruction cache is tight.
+template <int MODE>
 __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t brw, uint32_t biw,
-                                              bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc) {
+                                              bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc,
+                                              bool dual_rt = false) {
+    const bool dual = MODE == 2 ? dual_rt : MODE == 1;
     const bool ca = (a.ra >> 31) != 0;
     const uint32_t ar = a.ra & kMaskA, ai = a.ia & kMaskA, bra = brw & kMaskA, bia = biw & kMaskA;
     const uint32_t ad = (a.ra >> kShiftD) & kMaskD, adi = (a.ia >> kShiftD) & kMaskD;
@@ -359,10 +363,11 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
         uint32_t f = 0, pc = 0, pr = 0;
         bool und = false;
 #pragma unroll
-        for (int o = 0; o < (DUAL ? 2 : 1); ++o) {
-            // DUAL: o = 0 is (x, y), o = 1 is (y, x); otherwise the gated one
-            const bool g = DUAL ? (o ? gy : gx) : (gx | gy);
-            const bool oy = DUAL ? (o == 1) : !gx;
+        for (int o = 0; o < (MODE == 0 ? 1 : 2); ++o) {
+            if (MODE == 2 && o == 1 && !dual) break;
+            // dual: o = 0 is (x, y), o = 1 is (y, x); otherwise the gated one
+            const bool g = dual ? (o ? gy : gx) : (gx | gy);
+            const bool oy = dual ? (o == 1) : !gx;
             const float d = oy ? yf : xf;
             const uint32_t dres = oy ? Y : X;
             const Window w = window(fabsf(d), c);
@@ -383,7 +388,7 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             const uint32_t e2 = (m2 & sel) ? tab_d(tab, add_mod(sD, tD, kModD)) : 0u;
             f |= (e1 | e2) ? (oy ? kEvDy : kEvDx) : 0u;
         }
-        if (!DUAL) f |= (gx & gy) ? kEvB : 0u;
+        if (!dual) f |= (gx & gy) ? kEvB : 0u;
         // an undecided product is counted whole on the exact path instead
         cnt += und ? 0u : pc;
         r16 += und ? 0u : pr;
@@ -905,7 +910,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         for (uint32_t k = 0; k < na; ++k) {
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
-            if (live) flags = eval_fast<DUAL>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
+            if (live) flags = eval_fast<DUAL ? 1 : 0>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
             if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
@@ -1033,8 +1038,8 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
             const bool cb = (b.rre & kCentralBit) != 0;
             for (uint32_t k = 0; k < na; ++k) {
                 const uint32_t flags =
-                    pair_dual(c) ? eval_fast<true>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc)
-                                 : eval_fast<false>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
+                    pair_dual(c) ? eval_fast<1>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc)
+                                 : eval_fast<0>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
                 if (flags)
                     add_event(acc, cached_event(flags, s_alpha[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab,
                                                 (uint32_t)n, &buf));
@@ -1444,10 +1449,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                         kb -= (int32_t)nb;
                     }
                     const AlphaHot a = list[ka], bh = list[na + kb];
-                    flags = dual ? eval_fast<true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0,
-                                                   c, s_tab, acc)
-                                 : eval_fast<false>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0,
-                                                    c, s_tab, acc);
+                    flags = eval_fast<2>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc, dual);
                 }
                 if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags)))
                     drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
@@ -1501,9 +1503,8 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
             const uint32_t ka = k / nb, kb = k - ka * nb;
             const AlphaHot a = s_list[ka], bh = s_list[na + kb];
             const uint32_t flags =
-                pair_dual(c) ? eval_fast<true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
-                             : eval_fast<false>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab,
-                                                acc);
+                pair_dual(c) ? eval_fast<1>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
+                             : eval_fast<0>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
             if (flags)
                 add_event(acc, merged_event(flags, a, bh, c, ka, kb, (uint32_t)S.l, S.row, s_tab,
                                             (uint32_t)cache.limit, &buf));
