@@ -24,6 +24,13 @@ Multi-GPU: replicas.  Rank r searches its own 512-root batch starting at
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                   [--no-plain] [--no-cpu] [--no-serving]
+  python bench.py --workload uneven [--intervals P] [--steps K] [--warmup W]
+
+--workload uneven times the batched uneven workload instead: a seeded prefix
+of P intervals (lengths log-uniform in [1, 512] roots, uniform starts, 10 %
+moved onto heavy roots) at LIMIT 10^7 in one hss_search_many call per step,
+under a CUDA graph with the autotuned kernel variant; the first intervals are
+also run on the plain path and must give the same per-interval counts.
 """
 import argparse
 import json
@@ -61,6 +68,11 @@ SERVE_SEED = 5
 SERVE_REQUESTS = 12
 SERVE_RATE = 10.0        # requests per second (Poisson)
 SERVE_MAX_LEN = 4096     # lengths log-uniform in [1, SERVE_MAX_LEN] roots
+
+# batched uneven workload (--workload uneven)
+UNEVEN_SEED = 4
+UNEVEN_INTERVALS = 64
+UNEVEN_PLAIN_CHECK = 4
 
 
 def logical_pairs(first, last, limit=LIMIT):
@@ -229,6 +241,55 @@ def serving(s, seed=SERVE_SEED, n_req=SERVE_REQUESTS, rate=SERVE_RATE, max_len=S
                     "latency includes queueing; p99 of 12 requests is their maximum"}
 
 
+def uneven_arm(args, rank, world, local_rank):
+    """Batched uneven workload (see the module docstring); replicas: rank r
+    takes the intervals of seed UNEVEN_SEED + r."""
+    import hss
+    intervals = hss.uneven_intervals(UNEVEN_SEED + rank, args.intervals, LIMIT)
+    pairs = sum(logical_pairs(a, b) for a, b in intervals)
+    s = hss.Search(LIMIT, device=local_rank, use_graph=1)
+    chosen, _ = s.autotune(FIRST, FIRST + 63)
+    for _ in range(args.warmup):
+        s.search_many(intervals)
+    steps = []
+    with Clocks(local_rank) as clk:
+        for _ in range(args.steps):
+            t = time.time()
+            per, total = s.search_many(intervals)
+            steps.append((total, time.time() - t))
+    clocks = clk.summary()
+    dev_ms = sum(r.counts["kernel_ms"] for r, _ in steps) / args.steps
+    e2e_ms = 1e3 * sum(w for _, w in steps) / args.steps
+    c = steps[-1][0].counts
+    # plain path on the first intervals: same per-interval counts
+    check = intervals[:UNEVEN_PLAIN_CHECK]
+    plain_ms, same = 0.0, True
+    for (a, b), counts in zip(check, per):
+        r = s.search(a, b, mode="plain")
+        plain_ms += r.counts["kernel_ms"]
+        same &= all(r.counts[k] == counts[k] for k in ("pairs", "candidates", "products", "processed"))
+    plain_pairs = sum(logical_pairs(a, b) for a, b in check)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC + " (batched uneven workload)", "value": world * pairs / (dev_ms * 1e-3), "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded search intervals; no dataset)",
+            "config": {"workload": f"uneven: {len(intervals)} intervals of seed {UNEVEN_SEED}, lengths log-uniform "
+                                   f"in [1, 512] roots, 10 % heavy starts, LIMIT={LIMIT}",
+                       "limit": LIMIT, "intervals": len(intervals), "pairs": pairs, "graph": True,
+                       "autotuned": {k: chosen[k] for k in ("block_threads", "ctas_per_sm", "item_target")}},
+            "e2e": {"value": world * pairs / (e2e_ms * 1e-3), "unit": UNIT,
+                    "h2d_bytes_per_step": c["h2d_bytes"], "d2h_bytes_per_step": c["d2h_bytes"]},
+            "plain": {"intervals": len(check), "value": plain_pairs / (plain_ms * 1e-3), "unit": UNIT,
+                      "counts_equal": bool(same)},
+            "gpu_launches": sum(r.counts["launches"] for r, _ in steps),
+            "graph_launches": sum(r.counts["graph_launches"] for r, _ in steps),
+            "clocks": clocks}))
+    s.close()
+    return 0
+
+
 def our_arm(args, rank, world, local_rank):
     import hss
     dist = None
@@ -345,6 +406,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--workload", default="batch", choices=["batch", "uneven"])
+    ap.add_argument("--intervals", type=int, default=UNEVEN_INTERVALS)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
@@ -353,6 +416,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return reference_arm(args, rank, world)
+    if args.workload == "uneven":
+        return uneven_arm(args, rank, world, local_rank)
     return our_arm(args, rank, world, local_rank)
 
 

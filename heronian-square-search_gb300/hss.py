@@ -300,3 +300,44 @@ def partition_rows(limit: int, first: int, last: int, parts: int) -> List[Tuple[
         out.append((lo, hi))
         lo = hi + 1
     return out
+
+
+def branch_weight(l: int) -> int:
+    """prod (4e + 1) over the primes p = 1 mod 4 dividing l with exponent e
+    (experiments/heavy/gpu_search_v36.cu:51-56), by trial division."""
+    w, p = 1, 2
+    while p * p <= l:
+        if l % p == 0:
+            e = 0
+            while l % p == 0:
+                l //= p
+                e += 1
+            if p % 4 == 1:
+                w *= 4 * e + 1
+        p += 1 if p == 2 else 2
+    if l > 1 and l % 4 == 1:
+        w *= 5
+    return w
+
+
+def uneven_intervals(seed: int, count: int, limit: int, max_len: int = 512, heavy_fraction: float = 0.1,
+                     heavy_weight: int = 100) -> List[Tuple[int, int]]:
+    """The batched uneven workload: `count` intervals with lengths
+    log-uniform in [1, max_len] roots and starts uniform in
+    [1, limit - max_len]; a `heavy_fraction` of the starts is moved onto the
+    next root at or after it whose branch weight reaches `heavy_weight` (the
+    reference's heavy threshold, experiments/heavy/heavy_queue.py:13).
+    Deterministic in `seed`."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(count):
+        length = min(max(int(math.exp(rng.uniform(0.0, math.log(max_len)))), 1), max_len)
+        start = rng.randint(1, max(limit - max_len, 1))
+        if rng.random() < heavy_fraction:
+            while start < limit - max_len and branch_weight(start) < heavy_weight:
+                start += 1
+        last = min(start + length - 1, limit)
+        out.append((start, last))
+    return out
