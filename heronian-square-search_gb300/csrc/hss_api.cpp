@@ -634,7 +634,7 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     h->exact_cap = 1u << 24;
     if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
         (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
-        (s = device_alloc(h, &h->d_big, h->big_cap)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
+        (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
         (s = ensure_rows(h, 1024))) {
         hss_close(h);
         return s;

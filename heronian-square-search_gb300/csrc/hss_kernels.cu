@@ -1137,49 +1137,6 @@ __device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, u
     xi = outi;
 }
 
-// List entry k of group g multiplied out in float and residues (the same
-// decode as group_value; the exact value is rebuilt only for exact work).
-__device__ void group_value_hot(const DeviceCache& cache, const Group& g, uint32_t k, AlphaHot& out) {
-    float xr = g.scale_f, xi = 0.f;
-    uint32_t rr = g.scale_res, ri = 0u;
-    uint32_t i = 0;
-    const bool central = k >= g.free_count;
-    if (!central) {
-        while (k >= g.block[i]) {
-            k -= g.block[i];
-            ++i;
-        }
-    } else {
-        i = g.count;
-    }
-    auto mul = [&](const HotRec& v) {
-        const float nr = xr * v.re - xi * v.im, ni = xr * v.im + xi * v.re;
-        uint32_t yr, yi;
-        res_mul(rr, ri, v.rre & kResMask, v.rim, yr, yi);
-        xr = nr;
-        xi = ni;
-        rr = yr;
-        ri = yi;
-    };
-    for (uint32_t j = 0; j < i; ++j) mul(cache.pp_hot[g.base[j] + 2 * g.e[j]]);
-    if (i < g.count) {
-        uint32_t r = k / g.suffix[i];
-        uint32_t rem = k - r * g.suffix[i];
-        uint32_t digits[kMaxTerms];
-        for (uint32_t j = g.count - 1; j > i; --j) {
-            uint32_t s = 4 * g.e[j] + 1;
-            digits[j] = rem % s;
-            rem /= s;
-        }
-        digits[i] = r;
-        for (uint32_t j = i; j < g.count; ++j) mul(cache.pp_hot[g.base[j] + digits[j]]);
-    }
-    out.re = xr;
-    out.im = xi;
-    out.ra = rr | (central ? kCentralBit : 0u);
-    out.ia = ri;
-}
-
 // One event of a shared-prime pair: list entries ka (alpha side) and kb.
 __device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, AlphaHot bh, PairCtx c, uint32_t ka,
                                               uint32_t kb, uint32_t l, uint32_t row, const uint8_t* tab,
@@ -1266,7 +1223,7 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
 // sizes, the float/residue form of the group-0 scale 2 fixed(l) fixed(m), and
 // the pair constants.  state: 0 none, 1 fits a warp slice, 2 big, 3 unusable.
 constexpr uint32_t kDescTerms = 10;  // l, m <= 3e7 have at most 5 split primes each
-struct PairDesc {
+struct __align__(16) PairDesc {
     PairCtx ctx;
     uint32_t base[2][kDescTerms];
     uint32_t free_count[2];
@@ -1278,6 +1235,8 @@ struct PairDesc {
     uint8_t state;
     uint8_t cc;  // bit 0: the all-central product is a candidate; bit 1: it passes mod 16
 };
+static_assert(sizeof(PairDesc) <= kBigEntryWords * 16 && sizeof(PairDesc) % 16 == 0,
+              "a descriptor fits one big-queue entry");
 
 __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, PairDesc& D, uint32_t cap) {
     MergedShared S;
@@ -1287,7 +1246,7 @@ __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint
     D.row = q.z;
     D.state = S.ok == 1 ? 1 : (S.ok == 2 ? 2 : 3);
     if (S.g[0].count > kDescTerms || S.g[1].count > kDescTerms) D.state = 3;
-    if (D.state != 1) return;
+    if (D.state == 3) return;
     for (int g = 0; g < 2; ++g) {
         D.count[g] = (uint8_t)S.g[g].count;
         D.free_count[g] = S.g[g].free_count;
@@ -1360,7 +1319,7 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
 // to the big-pair queue (one CTA per pair).
 constexpr uint32_t kPairWarps = 4;
 __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ PairDesc s_desc[kPairWarps][32];
+    __shared__ __align__(16) PairDesc s_desc[kPairWarps][32];
     __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
     __shared__ uint64_t s_queue[kPairWarps][kQueue];
     // dynamic (static use is near 48 KB): root requests, then the tables
@@ -1383,11 +1342,15 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             const uint4 e = buf.merged_queue[qi];
             pair_desc_setup(cache, buf.row_info[e.z], e, desc[lane], kWarpListCap);
             if (desc[lane].state == 2) {
+                // the descriptor goes with the pair: the big kernel sets nothing up
                 unsigned int idx = atomicAdd(buf.big_count, 1u);
-                if (idx < buf.big_cap)
-                    buf.big_queue[idx] = e;
-                else
+                if (idx < buf.big_cap) {
+                    const uint4* src = reinterpret_cast<const uint4*>(&desc[lane]);
+                    uint4* dst = buf.big_queue + (size_t)idx * kBigEntryWords;
+                    for (uint32_t w = 0; w < sizeof(PairDesc) / 16; ++w) dst[w] = src[w];
+                } else {
                     atomicOr(buf.error_flags, 2u);
+                }
             } else if (desc[lane].state == 3) {
                 atomicOr(buf.error_flags, 2u);
             }
@@ -1462,54 +1425,60 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
     }
 }
 
-// Shared-prime pairs too big for a warp: one CTA per pair, events handled by
-// the lane that raised them.
+// Shared-prime pairs too big for a warp: one CTA per pair, from the
+// descriptor the warp kernel left in the big queue (so every thread builds
+// list entries at once); events are handled by the lane that raised them.
 __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ MergedShared S;
+    __shared__ PairDesc D;
     __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
     __shared__ __align__(16) uint8_t s_tab[kTableBytes];
     for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
     const uint32_t count = min(*buf.big_count, buf.big_cap);
     for (uint32_t qi = blockIdx.x; qi < count; qi += gridDim.x) {
         __syncthreads();
-        const uint4 e = buf.big_queue[qi];
-        const RowInfo& R = buf.row_info[e.z];
-        if (threadIdx.x == 0) {
-            merged_setup(cache, R, e, S, kMergedListCap);
-            uint32_t cc_c, cc_r;
-            S.ctx = make_ctx(R, e.y, cc_c, cc_r, 0x1p-16f);
-            S.cc_cand = cc_c;
-            S.cc_r16 = cc_r;
-            if (S.ok != 1) atomicOr(buf.error_flags, 2u);
-        }
+        if (threadIdx.x < sizeof(PairDesc) / 16)
+            reinterpret_cast<uint4*>(&D)[threadIdx.x] = buf.big_queue[(size_t)qi * kBigEntryWords + threadIdx.x];
         __syncthreads();
-        if (S.ok != 1) continue;
-        const uint32_t na = S.g[0].free_count + 1, nb = S.g[1].free_count + 1;
+        const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1;
+        if (na + nb > kMergedListCap) {
+            if (threadIdx.x == 0) atomicOr(buf.error_flags, 2u);
+            continue;
+        }
         for (uint32_t k = threadIdx.x; k < na + nb; k += kMergedThreads) {
             const int side = k < na ? 0 : 1;
-            const uint32_t idx = side ? k - na : k;
-            group_value_hot(cache, S.g[side], idx, s_list[k]);
+            desc_value_hot(cache, D, side, side ? k - na : k, s_list[k]);
         }
         __syncthreads();
         Acc acc{0, 0, 0, 0, 0, 0};
         if (threadIdx.x == 0) {
             acc.prod += 1;
-            acc.cand += S.cc_cand;
-            acc.r16 += S.cc_r16;
+            acc.cand += D.cc & 1u;
+            acc.r16 += (D.cc >> 1) & 1u;
         }
-        const PairCtx c = S.ctx;
+        const PairCtx c = D.ctx;
+        const uint32_t l = D.l, row = D.row;
         const uint32_t total = na * nb;
+        const float rcp = 1.0f / (float)nb;
         for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
-            const uint32_t ka = k / nb, kb = k - ka * nb;
+            uint32_t ka = (uint32_t)((float)k * rcp);
+            int32_t kb = (int32_t)k - (int32_t)(ka * nb);
+            while (kb < 0) {
+                --ka;
+                kb += (int32_t)nb;
+            }
+            while (kb >= (int32_t)nb) {
+                ++ka;
+                kb -= (int32_t)nb;
+            }
             const AlphaHot a = s_list[ka], bh = s_list[na + kb];
             const uint32_t flags =
                 pair_dual(c) ? eval_fast<1>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
                              : eval_fast<0>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
             if (flags)
-                add_event(acc, merged_event(flags, a, bh, c, ka, kb, (uint32_t)S.l, S.row, s_tab,
+                add_event(acc, merged_event(flags, a, bh, c, ka, (uint32_t)kb, l, row, s_tab,
                                             (uint32_t)cache.limit, &buf));
         }
-        flush_acc(acc, &buf.rows[S.row], true);
+        flush_acc(acc, &buf.rows[row], true);
     }
 }
 

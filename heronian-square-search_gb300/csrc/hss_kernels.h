@@ -46,6 +46,9 @@ struct ExactItem {
     uint32_t kind, a, b, l, m, row, pad0, pad1;
 };
 
+// 16-byte words of one big_queue entry.
+constexpr uint32_t kBigEntryWords = 12;
+
 // Device buffers one search call writes.
 struct LaunchBuffers {
     RowCounts* rows;            // [n_rows]
@@ -57,7 +60,8 @@ struct LaunchBuffers {
     uint32_t merged_cap;
     unsigned int* next_item;    // work-queue cursor of the batched kernel
     unsigned int* error_flags;  // bit 0: shared-prime queue full; 1: pair lists over capacity; 2: exact queue full
-    uint4* big_queue;           // shared-prime pairs too big for one warp's lists
+    uint4* big_queue;           // shared-prime pairs too big for one warp's lists: kBigEntryWords
+                                // words each (the pair's descriptor, set up by the warp kernel)
     unsigned int* big_count;
     uint32_t big_cap;
     const uint8_t* tables;      // kTableBytes residue tables

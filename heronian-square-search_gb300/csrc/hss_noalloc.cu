@@ -37,7 +37,7 @@ using namespace hss;
 constexpr uint32_t kNaRows = 64;          // root rows per call
 constexpr uint32_t kNaItems = 8192;       // work items per call
 constexpr uint32_t kNaMerged = 1u << 20;  // pairs sharing a split prime per call
-constexpr uint32_t kNaBig = 1u << 14;     // of which too big for one warp
+constexpr uint32_t kNaBig = 1u << 13;     // of which too big for one warp
 constexpr uint32_t kNaExact = 1u << 16;   // exact work items per call
 constexpr uint32_t kNaHits = 4096;        // hits kept per call (as the reference, gpu_search_v42.cu:177-178)
 constexpr uint32_t kNaCtrl = 8;
@@ -50,7 +50,7 @@ constexpr size_t kOffHits = align256(kOffRowInfo + kNaRows * sizeof(RowInfo));
 constexpr size_t kOffItems = align256(kOffHits + kNaHits * sizeof(DevHit));
 constexpr size_t kOffMerged = align256(kOffItems + kNaItems * sizeof(WorkItem));
 constexpr size_t kOffBig = align256(kOffMerged + (size_t)kNaMerged * sizeof(uint4));
-constexpr size_t kOffExact = align256(kOffBig + kNaBig * sizeof(uint4));
+constexpr size_t kOffExact = align256(kOffBig + (size_t)kNaBig * kBigEntryWords * sizeof(uint4));
 constexpr size_t kNoAllocBytes = align256(kOffExact + kNaExact * sizeof(ExactItem));
 static_assert(kNoAllocBytes <= (24u << 20), "scratch stays within 24 MiB");
 
