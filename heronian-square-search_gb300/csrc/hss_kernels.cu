@@ -373,19 +373,20 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             const Window w = window(fabsf(d), c);
             und |= g & w.und;
             const bool ok = g & !w.und;
+            // z = S - t and S + t for t = |d|: S -+ d, swapped when d < 0
             const bool neg = d < 0.f;
             const uint32_t dA = dres % kModA;
-            const uint32_t tA = neg ? (dA ? kModA - dA : 0u) : dA;
-            const uint32_t z1 = sub_mod(sA, tA, kModA), z2 = add_mod(sA, tA, kModA);
+            const uint32_t uA = sub_mod(sA, dA, kModA), vA = add_mod(sA, dA, kModA);
+            const uint32_t z1 = neg ? vA : uA, z2 = neg ? uA : vA;
             const uint32_t m1 = (ok & w.in1) ? tab[kTabA + z1] : 0u;
             const uint32_t m2 = (ok & w.in2) ? tab[kTabA + z2] : 0u;
             pc += ok ? (uint32_t)w.in1 + (uint32_t)w.in2 : 0u;
             pr += (m1 & 1u) + (m2 & 1u);
             // field D of the terms that passed field A
             const uint32_t dD = (oy ? YD : XD) % kModD;
-            const uint32_t tD = neg ? (dD ? kModD - dD : 0u) : dD;
-            const uint32_t e1 = (m1 & sel) ? tab_d(tab, sub_mod(sD, tD, kModD)) : 0u;
-            const uint32_t e2 = (m2 & sel) ? tab_d(tab, add_mod(sD, tD, kModD)) : 0u;
+            const uint32_t uD = sub_mod(sD, dD, kModD), vD = add_mod(sD, dD, kModD);
+            const uint32_t e1 = (m1 & sel) ? tab_d(tab, neg ? vD : uD) : 0u;
+            const uint32_t e2 = (m2 & sel) ? tab_d(tab, neg ? uD : vD) : 0u;
             f |= (e1 | e2) ? (oy ? kEvDy : kEvDx) : 0u;
         }
         if (!dual) f |= (gx & gy) ? kEvB : 0u;
@@ -1381,7 +1382,9 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             const PairCtx c = D.ctx;
             const uint32_t l = D.l, row = D.row;
             const uint32_t total = na * nb;
-            const float rcp = 1.0f / (float)nb;
+            // lane's (ka, kb) for k = base + lane, advanced by 32 = q32 nb + r32 per round
+            uint32_t ka = lane / nb, kb = lane - ka * nb;
+            const uint32_t q32 = 32u / nb, r32 = 32u - q32 * nb;
             auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
                 if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
@@ -1397,25 +1400,19 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
             };
             const bool dual = pair_dual(c);
             for (uint32_t base = 0; base < total; base += 32) {
-                const uint32_t k = base + lane;
-                uint32_t flags = 0, ka = 0;
-                int32_t kb = 0;
-                if (k < total) {
-                    ka = (uint32_t)((float)k * rcp);
-                    kb = (int32_t)k - (int32_t)(ka * nb);
-                    while (kb < 0) {
-                        --ka;
-                        kb += (int32_t)nb;
-                    }
-                    while (kb >= (int32_t)nb) {
-                        ++ka;
-                        kb -= (int32_t)nb;
-                    }
+                uint32_t flags = 0;
+                if (base + lane < total) {
                     const AlphaHot a = list[ka], bh = list[na + kb];
                     flags = eval_fast<2>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc, dual);
                 }
-                if (queue_push(q, qn, flags != 0, make_event((uint32_t)kb, ka, flags)))
+                if (queue_push(q, qn, flags != 0, make_event(kb, ka, flags)))
                     drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
+                ka += q32;
+                kb += r32;
+                if (kb >= nb) {
+                    kb -= nb;
+                    ++ka;
+                }
             }
             while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
             __syncwarp();
@@ -1458,25 +1455,22 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         const PairCtx c = D.ctx;
         const uint32_t l = D.l, row = D.row;
         const uint32_t total = na * nb;
-        const float rcp = 1.0f / (float)nb;
+        // thread's (ka, kb) for k = threadIdx.x + j kMergedThreads, advanced incrementally
+        uint32_t ka = threadIdx.x / nb, kb = threadIdx.x - ka * nb;
+        const uint32_t qs = kMergedThreads / nb, rs = kMergedThreads - qs * nb;
         for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
-            uint32_t ka = (uint32_t)((float)k * rcp);
-            int32_t kb = (int32_t)k - (int32_t)(ka * nb);
-            while (kb < 0) {
-                --ka;
-                kb += (int32_t)nb;
-            }
-            while (kb >= (int32_t)nb) {
-                ++ka;
-                kb -= (int32_t)nb;
-            }
             const AlphaHot a = s_list[ka], bh = s_list[na + kb];
             const uint32_t flags =
                 pair_dual(c) ? eval_fast<1>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
                              : eval_fast<0>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
             if (flags)
-                add_event(acc, merged_event(flags, a, bh, c, ka, (uint32_t)kb, l, row, s_tab,
-                                            (uint32_t)cache.limit, &buf));
+                add_event(acc, merged_event(flags, a, bh, c, ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf));
+            ka += qs;
+            kb += rs;
+            if (kb >= nb) {
+                kb -= nb;
+                ++ka;
+            }
         }
         flush_acc(acc, &buf.rows[row], true);
     }
