@@ -626,13 +626,13 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
         h->seg_off = std::move(hc.seg_off);
         h->spf = std::move(hc.spf);
     }
-    uint8_t tables[kTableBytes];
-    build_residue_tables(tables);
+    std::vector<uint8_t> tables(kTableTotalBytes);
+    build_residue_tables(tables.data());
     h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
     h->merged_cap = (uint32_t)kMergedCap;
     h->big_cap = 1u << 20;
     h->exact_cap = 1u << 24;
-    if ((s = upload(h, &h->d_tables, tables, kTableBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
+    if ((s = upload(h, &h->d_tables, tables.data(), kTableTotalBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
         (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
         (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
         (s = ensure_rows(h, 1024))) {

@@ -51,6 +51,7 @@ using i128 = __int128;
 constexpr uint32_t kSqA = kModA * kModA;
 constexpr uint32_t kSqD = kModD * kModD;
 constexpr uint32_t kTabA = 0, kTabD = kModA;  // byte offsets: field-A bytes, then the field-D bit set
+constexpr uint32_t kTabD2 = 2 * kModA;        // field-D bit set in the wide copy
 constexpr uint32_t kSlices = 8;            // plain kernel: blocks per row
 constexpr uint32_t kPlainThreads = 128;    // plain kernel: threads per block
 constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
@@ -148,13 +149,15 @@ __device__ __forceinline__ uint32_t tab_at(const uint8_t* tab, uint32_t base, ui
     return index_ok(i, n, err) ? tab[base + i] : 0u;
 }
 
-// Bit z of the field-D table: z is a fourth-power residue mod 17, 37 and 73.
-__device__ __forceinline__ uint32_t tab_d(const uint8_t* tab, uint32_t z) {
-    return (reinterpret_cast<const uint32_t*>(tab + kTabD)[z >> 5] >> (z & 31u)) & 1u;
+// Bit z of a field-D bit set: z is a fourth-power residue mod 17, 37 and 73.
+__device__ __forceinline__ uint32_t tab_d(const uint32_t* bits, uint32_t z) { return (bits[z >> 5] >> (z & 31u)) & 1u; }
+
+__device__ __forceinline__ const uint32_t* tab_d_bits(const uint8_t* tab, uint32_t offset) {
+    return reinterpret_cast<const uint32_t*>(tab + offset);
 }
 
-__device__ __forceinline__ uint32_t tab_d_at(const uint8_t* tab, uint32_t z, unsigned int* err) {
-    return index_ok(z, kModD, err) ? tab_d(tab, z) : 0u;
+__device__ __forceinline__ uint32_t tab_d_at(const uint32_t* bits, uint32_t z, unsigned int* err) {
+    return index_ok(z, kModD, err) ? tab_d(bits, z) : 0u;
 }
 
 // ----------------------------------------------------------- 256-bit check
@@ -237,7 +240,7 @@ __device__ void exact_test_d(const ExactPair& p, i128 d, i128 area4, uint32_t& c
     if (((uint32_t)z & 15u) > 1u) return;
     ++r16;
     if (!(tab[kTabA + mod_u128_small(z, kModA)] & ((p.flags & 2u) ? 4u : 2u))) return;
-    if (!tab_d(tab, mod_u128_small(z, kModD))) return;
+    if (!tab_d(tab_d_bits(tab, kTabD), mod_u128_small(z, kModD))) return;
     double zd = (double)(uint64_t)(z >> 64) * 18446744073709551616.0 + (double)(uint64_t)z;
     uint64_t root = (uint64_t)sqrt(sqrt(zd));
     while (root > 0 && (u128)root * root * root * root > z) --root;
@@ -334,10 +337,13 @@ __device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t m) 
 // orientation and raises kEvB if both ever pass, so it stays exact regardless.
 // MODE 0: non-dual pair, 1: dual pair, 2: either (dual_rt), one code copy for
 // kernels whose lanes meet both kinds and whose instruction cache is tight.
-template <int MODE>
+// WIDE: `tab` is the wide copy (tables over two periods), so z residues are
+// indexed as S + d and S + M - d without a reduction; otherwise the compact one.
+template <int MODE, bool WIDE = false>
 __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t brw, uint32_t biw,
                                               bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc,
                                               bool dual_rt = false) {
+    const uint32_t* tabd = tab_d_bits(tab, WIDE ? kTabD2 : kTabD);
     const bool dual = MODE == 2 ? dual_rt : MODE == 1;
     const bool ca = (a.ra >> 31) != 0;
     const uint32_t ar = a.ra & kMaskA, ai = a.ia & kMaskA, bra = brw & kMaskA, bia = biw & kMaskA;
@@ -376,7 +382,8 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             // z = S - t and S + t for t = |d|: S -+ d, swapped when d < 0
             const bool neg = d < 0.f;
             const uint32_t dA = dres % kModA;
-            const uint32_t uA = sub_mod(sA, dA, kModA), vA = add_mod(sA, dA, kModA);
+            const uint32_t uA = WIDE ? sA + kModA - dA : sub_mod(sA, dA, kModA);
+            const uint32_t vA = WIDE ? sA + dA : add_mod(sA, dA, kModA);
             const uint32_t z1 = neg ? vA : uA, z2 = neg ? uA : vA;
             const uint32_t m1 = (ok & w.in1) ? tab[kTabA + z1] : 0u;
             const uint32_t m2 = (ok & w.in2) ? tab[kTabA + z2] : 0u;
@@ -384,9 +391,10 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             pr += (m1 & 1u) + (m2 & 1u);
             // field D of the terms that passed field A
             const uint32_t dD = (oy ? YD : XD) % kModD;
-            const uint32_t uD = sub_mod(sD, dD, kModD), vD = add_mod(sD, dD, kModD);
-            const uint32_t e1 = (m1 & sel) ? tab_d(tab, neg ? vD : uD) : 0u;
-            const uint32_t e2 = (m2 & sel) ? tab_d(tab, neg ? uD : vD) : 0u;
+            const uint32_t uD = WIDE ? sD + kModD - dD : sub_mod(sD, dD, kModD);
+            const uint32_t vD = WIDE ? sD + dD : add_mod(sD, dD, kModD);
+            const uint32_t e1 = (m1 & sel) ? tab_d(tabd, neg ? vD : uD) : 0u;
+            const uint32_t e2 = (m2 & sel) ? tab_d(tabd, neg ? uD : vD) : 0u;
             f |= (e1 | e2) ? (oy ? kEvDy : kEvDx) : 0u;
         }
         if (!dual) f |= (gx & gy) ? kEvB : 0u;
@@ -492,9 +500,11 @@ __device__ __forceinline__ void sink_push(const EventSink& s, uint32_t kind) {
 // passes the field-A and field-D tables go to the root filter: left as
 // requests in `slots` while there is room, else scanned here; returns true
 // when such a scan found a possible root.
+// `tab` may be the compact or the wide table copy (field A's first period is
+// the same in both); field D is read from the compact copy in global memory.
 __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot& a, const HotRec& b,
                                           const PairCtx& c, uint32_t n_limit, const uint8_t* tab, RootReq* slots,
-                                          uint32_t& nreq, unsigned int* err) {
+                                          uint32_t& nreq, unsigned int* err, const uint32_t* gtabd) {
     const bool plus = o != p;
     const float fu = o ? a.re * b.im : a.re * b.re;
     const float fv = o ? a.im * b.re : a.im * b.im;
@@ -520,7 +530,7 @@ __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot
         const uint32_t zA = term ? add_mod(sA, tA, kModA) : sub_mod(sA, tA, kModA);
         if (!(tab_at(tab, kTabA, zA, kModA, err) & sel)) continue;
         const uint32_t zD = term ? add_mod(sD, tD, kModD) : sub_mod(sD, tD, kModD);
-        if (!tab_d_at(tab, zD, err)) continue;
+        if (!tab_d_at(gtabd, zD, err)) continue;
         uint32_t nlo, nhi;
         root_window(term ? c.sf + t : c.sf - t, c, n_limit, nlo, nhi);
         const uint32_t zres = zA | (zD << kShiftD);
@@ -582,7 +592,7 @@ __device__ __noinline__ uint4 general_event(uint32_t flags, AlphaHot a, HotRec b
                 if (w.in1) r16 += tab_at(tab, kTabA, sub_mod(sA, tA, kModA), kModA, err) & 1u;
                 if (w.in2) r16 += tab_at(tab, kTabA, add_mod(sA, tA, kModA), kModA, err) & 1u;
             }
-            if (deep_unit(p, o, a, b, c, n_limit, tab, slots, nreq, err)) {
+            if (deep_unit(p, o, a, b, c, n_limit, tab, slots, nreq, err, tab_d_bits(sink.buf->tables, kTabD))) {
                 if (slots)
                     passed |= 1u << (2 * p + o);
                 else
@@ -608,7 +618,8 @@ __device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a
     while (units) {
         const uint32_t u = __ffs(units) - 1;
         units &= units - 1;
-        if (deep_unit(u >> 1, u & 1u, a, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags)) {
+        if (deep_unit(u >> 1, u & 1u, a, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags,
+                      tab_d_bits(sink.buf->tables, kTabD))) {
             if (slots)
                 passed |= 1u << u;
             else
@@ -911,7 +922,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         for (uint32_t k = 0; k < na; ++k) {
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
-            if (live) flags = eval_fast<DUAL ? 1 : 0>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
+            if (live) flags = eval_fast<DUAL ? 1 : 0, true>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
             if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
@@ -937,7 +948,7 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
     PairCtx* wctx = s_wctx + warp * kChunk;
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
-    for (uint32_t i = tid; i < kTableBytes; i += NT) s_tab[i] = buf.tables[i];
+    for (uint32_t i = tid; i < kTable2Bytes; i += NT) s_tab[i] = buf.tables[kTableBytes + i];
     Acc acc{0, 0, 0, 0, 0, 0};
     for (;;) {
         __syncthreads();
@@ -1626,13 +1637,20 @@ void build_residue_tables(uint8_t* out) {
     for (uint32_t z = 0; z < kModD; ++z)
         if (r17[z % 17] && r37[z % 37] && r73[z % 73]) words[z >> 5] |= 1u << (z & 31u);
     memcpy(out + kTabD, words, sizeof words);
+    // wide copy: both tables over two periods
+    uint8_t* wide = out + kTableBytes;
+    for (uint32_t z = 0; z < 2 * kModA; ++z) wide[z] = out[kTabA + z % kModA];
+    uint32_t words2[kTabD2Words] = {};
+    for (uint32_t z = 0; z < 2 * kModD; ++z)
+        if ((words[(z % kModD) >> 5] >> ((z % kModD) & 31u)) & 1u) words2[z >> 5] |= 1u << (z & 31u);
+    memcpy(wide + kTabD2, words2, sizeof words2);
 }
 
 size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
     const uint32_t warps = (uint32_t)threads / 32;
     return (size_t)alpha_cap * sizeof(AlphaHot) +
            (size_t)warps * 32 * kRootsPerLane * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
-           (size_t)warps * 32 * kReqPerLane * sizeof(RootReq) + kTableBytes;
+           (size_t)warps * 32 * kReqPerLane * sizeof(RootReq) + kTable2Bytes;
 }
 
 // Compiled (threads, min CTAs per SM) variants of the persistent kernel; the

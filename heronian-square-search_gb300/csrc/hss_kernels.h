@@ -18,7 +18,14 @@ namespace hss {
 constexpr uint32_t kTabDWords = (kModD + 31) / 32;
 constexpr uint32_t kTableBytes = kModA + 4 * kTabDWords;
 static_assert(kModA % 4 == 0, "the bit set starts on a word");
-void build_residue_tables(uint8_t* out /* kTableBytes */);
+// Wide copy, after the compact one: tabA and the tabD bit set each repeated
+// over two periods (indices up to 2M - 1), so the persistent kernel indexes
+// them with S + d and S + M - d without reducing mod M.
+constexpr uint32_t kTabD2Words = (2 * kModD + 31) / 32;
+constexpr uint32_t kTable2Bytes = 2 * kModA + 4 * kTabD2Words;
+constexpr uint32_t kTableTotalBytes = kTableBytes + kTable2Bytes;
+static_assert(kTableBytes % 4 == 0, "the wide copy starts on a word");
+void build_residue_tables(uint8_t* out /* kTableTotalBytes */);
 
 // Constants of one root row, built on the host for every row of a launch
 // (so no kernel factors l): l, l^2, l^4, N^4, residues, the odd primes of l
@@ -64,7 +71,7 @@ struct LaunchBuffers {
                                 // words each (the pair's descriptor, set up by the warp kernel)
     unsigned int* big_count;
     uint32_t big_cap;
-    const uint8_t* tables;      // kTableBytes residue tables
+    const uint8_t* tables;      // kTableTotalBytes residue tables (compact, then wide)
     const RowInfo* row_info;    // [n_rows] constants of the launch's rows
     ExactItem* exact_queue;     // rare exact work (undecided products, possible hits)
     unsigned int* exact_count;
