@@ -1439,8 +1439,8 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
 __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
     __shared__ PairDesc D;
     __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
-    __shared__ __align__(16) uint8_t s_tab[kTableBytes];
-    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
+    extern __shared__ __align__(16) uint8_t s_tab[];  // kTable2Bytes, dynamic: the wide table copy
+    for (uint32_t i = threadIdx.x; i < kTable2Bytes; i += kMergedThreads) s_tab[i] = buf.tables[kTableBytes + i];
     const uint32_t count = min(*buf.big_count, buf.big_cap);
     for (uint32_t qi = blockIdx.x; qi < count; qi += gridDim.x) {
         __syncthreads();
@@ -1472,8 +1472,8 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
             const AlphaHot a = s_list[ka], bh = s_list[na + kb];
             const uint32_t flags =
-                pair_dual(c) ? eval_fast<1>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
-                             : eval_fast<0>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
+                pair_dual(c) ? eval_fast<1, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
+                             : eval_fast<0, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
             if (flags)
                 add_event(acc, merged_event(flags, a, bh, c, ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf));
             ka += qs;
@@ -1700,7 +1700,10 @@ cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const Launch
     merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    merged_big_kernel<<<ctas, kMergedThreads, 0, stream>>>(cache, buf);
+    e = cudaFuncSetAttribute((const void*)merged_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kTable2Bytes);
+    if (e != cudaSuccess) return e;
+    merged_big_kernel<<<ctas, kMergedThreads, kTable2Bytes, stream>>>(cache, buf);
     return cudaGetLastError();
 }
 
