@@ -24,16 +24,20 @@ pytestmark = [
 ]
 
 
-def _import(directory, name, argv=None):
-    saved_argv, saved_path = sys.argv, list(sys.path)
-    sys.argv = argv or [name + ".py"]
+def _import(directory, name, env=None):
+    """Imports a reference script as a module (its main() does not run) with
+    the arguments and environment its module level reads."""
+    saved_argv, saved_path, saved_env = sys.argv, list(sys.path), dict(os.environ)
+    sys.argv = [name + ".py"]
     sys.path.insert(0, str(directory))
-    os.environ.setdefault("GPU_IDS", "0")
+    os.environ.update(env or {})
     try:
         sys.modules.pop(name, None)
         return importlib.import_module(name)
     finally:
         sys.argv, sys.path[:] = saved_argv, saved_path
+        os.environ.clear()
+        os.environ.update(saved_env)
 
 
 def weight(l):
@@ -54,7 +58,7 @@ def weight(l):
 def test_stage_accepted_by_coverage_audit_and_queue():
     audit = _import(REFERENCE / "scripts", "coverage_audit")
     assert audit.gpu_complete(STAGE[0], STAGE[1], FIXTURES / "gpu-0-state.txt")
-    queue = _import(REFERENCE / "scripts", "gpu_queue")
+    queue = _import(REFERENCE / "scripts", "gpu_queue", {"GPU_IDS": "0"})
     assert queue.checkpoint_resume(STAGE[0], STAGE[1], FIXTURES / "gpu-0-state.txt") == STAGE[1] + 1
 
 
@@ -63,6 +67,6 @@ def test_heavy_range_accepted_by_coverage_audit_and_heavy_queue():
     covered = audit.heavy_covered(FIXTURES / f"{HEAVY_STEM}-state.txt")
     heavy = [l for l in range(HEAVY[0], HEAVY[1] + 1) if weight(l) >= 100]
     assert covered == [(l, l) for l in heavy]
-    queue = _import(REFERENCE / "experiments" / "heavy", "heavy_queue")
+    queue = _import(REFERENCE / "experiments" / "heavy", "heavy_queue", {"HEAVY_QUEUE_DEADLINE": "4102444800"})
     queue.ROOT = FIXTURES
     assert queue.complete(*HEAVY)
