@@ -134,3 +134,20 @@ def test_serving_results_same_alone_and_in_mix(searches):
             assert got["counts"][key] == want.counts[key], key
         assert sorted(got["hits"]) == sorted(want.hits)
         assert got["finished_ns"] >= got["admitted_ns"] >= got["submitted_ns"]
+
+
+def test_maximum_limit_rows(built):
+    """LIMIT at its maximum (3e7): the top rows, and the root below it with
+    the largest branch weight (29,995,225: 5625, so 2813 row values), per
+    row against the oracle in both modes."""
+    limit = 30_000_000
+    cases = [(29_999_000, 29_999_063), (29_995_225, 29_995_225)]
+    with Oracle(limit) as o, hss.Search(limit) as s:
+        for first, last in cases:
+            want = o.search(first, last)
+            for mode in ("batched", "plain"):
+                got = s.search(first, last, mode=mode, rows=True)
+                for key in FIELDS:
+                    assert got.counts[key] == want[key], (first, mode, key)
+                assert got.row_candidates == want["row_candidates"]
+                assert sorted(got.hits) == sorted(want["hits"])
