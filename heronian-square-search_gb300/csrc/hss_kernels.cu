@@ -486,6 +486,7 @@ __device__ __forceinline__ void push_exact(const LaunchBuffers& buf, uint32_t ki
 struct EventSink {
     const LaunchBuffers* buf;
     uint32_t a, b, l, m, row, shared_prime;
+    const uint32_t* tabd;  // field-D bit set of the kernel's shared-memory table copy
 };
 
 __device__ __forceinline__ void sink_push(const EventSink& s, uint32_t kind) {
@@ -501,10 +502,10 @@ __device__ __forceinline__ void sink_push(const EventSink& s, uint32_t kind) {
 // requests in `slots` while there is room, else scanned here; returns true
 // when such a scan found a possible root.
 // `tab` may be the compact or the wide table copy (field A's first period is
-// the same in both); field D is read from the compact copy in global memory.
+// the same in both); `tabd` is that copy's field-D bit set.
 __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot& a, const HotRec& b,
                                           const PairCtx& c, uint32_t n_limit, const uint8_t* tab, RootReq* slots,
-                                          uint32_t& nreq, unsigned int* err, const uint32_t* gtabd) {
+                                          uint32_t& nreq, unsigned int* err, const uint32_t* tabd) {
     const bool plus = o != p;
     const float fu = o ? a.re * b.im : a.re * b.re;
     const float fv = o ? a.im * b.re : a.im * b.im;
@@ -530,7 +531,7 @@ __device__ __forceinline__ bool deep_unit(uint32_t p, uint32_t o, const AlphaHot
         const uint32_t zA = term ? add_mod(sA, tA, kModA) : sub_mod(sA, tA, kModA);
         if (!(tab_at(tab, kTabA, zA, kModA, err) & sel)) continue;
         const uint32_t zD = term ? add_mod(sD, tD, kModD) : sub_mod(sD, tD, kModD);
-        if (!tab_d_at(gtabd, zD, err)) continue;
+        if (!tab_d_at(tabd, zD, err)) continue;
         uint32_t nlo, nhi;
         root_window(term ? c.sf + t : c.sf - t, c, n_limit, nlo, nhi);
         const uint32_t zres = zA | (zD << kShiftD);
@@ -592,7 +593,7 @@ __device__ __noinline__ uint4 general_event(uint32_t flags, AlphaHot a, HotRec b
                 if (w.in1) r16 += tab_at(tab, kTabA, sub_mod(sA, tA, kModA), kModA, err) & 1u;
                 if (w.in2) r16 += tab_at(tab, kTabA, add_mod(sA, tA, kModA), kModA, err) & 1u;
             }
-            if (deep_unit(p, o, a, b, c, n_limit, tab, slots, nreq, err, tab_d_bits(sink.buf->tables, kTabD))) {
+            if (deep_unit(p, o, a, b, c, n_limit, tab, slots, nreq, err, sink.tabd)) {
                 if (slots)
                     passed |= 1u << (2 * p + o);
                 else
@@ -619,7 +620,7 @@ __device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a
         const uint32_t u = __ffs(units) - 1;
         units &= units - 1;
         if (deep_unit(u >> 1, u & 1u, a, b, c, n_limit, tab, slots, nreq, sink.buf->error_flags,
-                      tab_d_bits(sink.buf->tables, kTabD))) {
+                      sink.tabd)) {
             if (slots)
                 passed |= 1u << u;
             else
@@ -636,9 +637,9 @@ __device__ __forceinline__ uint4 process_event(uint32_t flags, const AlphaHot& a
 // With `slots`, x also carries the root requests left (bits 16-19) and the
 // orientations already found possible (bits 20-23).
 __device__ __noinline__ uint2 cached_event(uint32_t flags, AlphaHot a, HotRec b, PairCtx c, uint32_t ka, uint32_t j,
-                                              uint32_t l, uint32_t row, const uint8_t* tab, uint32_t limit,
+                                              uint32_t l, uint32_t row, const uint8_t* tab, uint32_t tabd_ofs, uint32_t limit,
                                               const LaunchBuffers* buf, RootReq* slots = nullptr) {
-    const EventSink sink{buf, ka, j, l, pair_m(c), row, 0u};
+    const EventSink sink{buf, ka, j, l, pair_m(c), row, 0u, tab_d_bits(tab, tabd_ofs)};
     const uint4 r = process_event(flags, a, b, c, limit, tab, sink, slots);
     return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
@@ -884,7 +885,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
         if (!index_ok(k, na, buf.error_flags) || !index_ok(slot, 32 * kRootsPerLane, buf.error_flags)) return 0u;
         const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], cache.hot[j], wctx[slot], a0 + k, j,
-                                     (uint32_t)l, row, s_tab, (uint32_t)cache.limit, &buf, slots);
+                                     (uint32_t)l, row, s_tab, kTabD2, (uint32_t)cache.limit, &buf, slots);
         acc.cand += r.x & 0xFFFFu;
         acc.r16 += r.y;
         return r.x >> 16;
@@ -1053,7 +1054,7 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
                     pair_dual(c) ? eval_fast<1>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc)
                                  : eval_fast<0>(s_alpha[k], b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
                 if (flags)
-                    add_event(acc, cached_event(flags, s_alpha[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab,
+                    add_event(acc, cached_event(flags, s_alpha[k], b, c, a0 + k, j, (uint32_t)l, row, s_tab, kTabD,
                                                 (uint32_t)n, &buf));
             }
         }
@@ -1152,9 +1153,10 @@ __device__ __forceinline__ void res_mul(uint32_t ar, uint32_t ai, uint32_t br, u
 // One event of a shared-prime pair: list entries ka (alpha side) and kb.
 __device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, AlphaHot bh, PairCtx c, uint32_t ka,
                                               uint32_t kb, uint32_t l, uint32_t row, const uint8_t* tab,
-                                              uint32_t limit, const LaunchBuffers* buf, RootReq* slots = nullptr) {
+                                              uint32_t tabd_ofs, uint32_t limit, const LaunchBuffers* buf,
+                                              RootReq* slots = nullptr) {
     const HotRec b{bh.re, bh.im, bh.ra, bh.ia};
-    const EventSink sink{buf, ka, kb, l, pair_m(c), row, 1u};
+    const EventSink sink{buf, ka, kb, l, pair_m(c), row, 1u, tab_d_bits(tab, tabd_ofs)};
     const uint4 r = process_event(flags, a, b, c, limit, tab, sink, slots);
     return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
@@ -1400,7 +1402,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
                 if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
                 const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], list[na + kb], c, ka, kb, l, row, s_tab,
-                                             (uint32_t)cache.limit, &buf, slots);
+                                             kTabD, (uint32_t)cache.limit, &buf, slots);
                 acc.cand += r.x & 0xFFFFu;
                 acc.r16 += r.y;
                 return r.x >> 16;
@@ -1475,7 +1477,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
                 pair_dual(c) ? eval_fast<1, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
                              : eval_fast<0, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
             if (flags)
-                add_event(acc, merged_event(flags, a, bh, c, ka, kb, l, row, s_tab, (uint32_t)cache.limit, &buf));
+                add_event(acc, merged_event(flags, a, bh, c, ka, kb, l, row, s_tab, kTabD2, (uint32_t)cache.limit, &buf));
             ka += qs;
             kb += rs;
             if (kb >= nb) {
