@@ -23,16 +23,17 @@
 // Counts are therefore exact and every hit is confirmed exactly and rechecked
 // in 256-bit arithmetic.
 //
-// The hot loop is branch-free per (alpha, beta) value pair.  Work that only
-// a few lanes need (deep residue filters, the fourth-root filter, undecided
+// The hot loop is branch-free per (alpha, beta) value pair and tests both
+// residue fields of every counted candidate.  Work that only a few lanes need
+// (the fourth-root filter of candidates that passed both fields, undecided
 // products, products whose both orientations pass the area test) is written
-// to a per-warp queue of events and processed 32 at a time with every lane
-// busy, outside the hot loop.
+// to a per-warp queue of events and processed 32 at a time, outside the hot
+// loop; the root filter's windows are then scanned by the whole warp.
 //
 // Work shapes.  batched_kernel is persistent: CTAs pull (row l, m-range)
-// items from a global cursor; per item the valid m-side records are compacted
-// into shared memory and processed in lockstep rounds against the row's
-// segment, also in shared memory.  plain_kernel keeps the reference's shape
+// items from a global cursor; per item the row's values are staged in shared
+// memory, and each warp walks the m-side records of 128 roots (read from the
+// cache, coalesced) in lockstep rounds against them.  plain_kernel keeps the reference's shape
 // (a block per (row, slice), one thread per pair).  merged_kernel (a warp per
 // pair) and merged_big_kernel (a CTA per pair) handle the pairs that share a
 // split prime (gpu_search_v42.cu:318-341).
