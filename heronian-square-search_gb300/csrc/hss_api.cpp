@@ -213,6 +213,7 @@ LaunchBuffers buffers(const hss_t* h, size_t row_offset) {
     b.exact_cap = h->exact_cap;
     b.big_queue = h->d_big;
     b.big_count = h->d_ctrl + 4;
+    b.big_next = h->d_ctrl + 6;
     b.big_cap = h->big_cap;
     return b;
 }
@@ -378,7 +379,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
         HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                     h->stream));
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, 2 * sizeof(unsigned int), h->stream));
-        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 3 * sizeof(unsigned int), h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[0], h->stream, rec));
         HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[1], h->stream, rec));
@@ -432,7 +433,7 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
             if (g) return g;
         }
         HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 1, 0, sizeof(unsigned int), h->stream));
-        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 2 * sizeof(unsigned int), h->stream));
+        HSS_CUDA(h, cudaMemsetAsync(h->d_ctrl + 4, 0, 3 * sizeof(unsigned int), h->stream));
         LaunchBuffers buf = buffers(h, b - first);
         std::array<cudaEvent_t, 3> ev;
         if (int e = take_events(h, &ev)) return e;

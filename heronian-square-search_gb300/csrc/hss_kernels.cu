@@ -1444,9 +1444,15 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
     __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
     extern __shared__ __align__(16) uint8_t s_tab[];  // kTable2Bytes, dynamic: the wide table copy
     for (uint32_t i = threadIdx.x; i < kTable2Bytes; i += kMergedThreads) s_tab[i] = buf.tables[kTableBytes + i];
+    __shared__ uint32_t s_qi;
     const uint32_t count = min(*buf.big_count, buf.big_cap);
-    for (uint32_t qi = blockIdx.x; qi < count; qi += gridDim.x) {
+    for (;;) {
+        // pairs are taken from a cursor: their sizes vary by orders of magnitude
         __syncthreads();
+        if (threadIdx.x == 0) s_qi = atomicAdd(buf.big_next, 1u);
+        __syncthreads();
+        const uint32_t qi = s_qi;
+        if (qi >= count) break;
         if (threadIdx.x < sizeof(PairDesc) / 16)
             reinterpret_cast<uint4*>(&D)[threadIdx.x] = buf.big_queue[(size_t)qi * kBigEntryWords + threadIdx.x];
         __syncthreads();

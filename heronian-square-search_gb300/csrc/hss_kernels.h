@@ -70,6 +70,7 @@ struct LaunchBuffers {
     uint4* big_queue;           // shared-prime pairs too big for one warp's lists: kBigEntryWords
                                 // words each (the pair's descriptor, set up by the warp kernel)
     unsigned int* big_count;
+    unsigned int* big_next;     // cursor of the big-pair kernel over big_queue
     uint32_t big_cap;
     const uint8_t* tables;      // kTableTotalBytes residue tables (compact, then wide)
     const RowInfo* row_info;    // [n_rows] constants of the launch's rows

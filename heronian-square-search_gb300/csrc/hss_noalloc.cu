@@ -159,6 +159,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     b.error_flags = ctrl + 3;
     b.big_queue = reinterpret_cast<uint4*>(base + kOffBig);
     b.big_count = ctrl + 4;
+    b.big_next = ctrl + 6;
     b.big_cap = kNaBig;
     b.exact_queue = reinterpret_cast<ExactItem*>(base + kOffExact);
     b.exact_count = ctrl + 5;
