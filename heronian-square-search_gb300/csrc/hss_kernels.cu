@@ -1438,13 +1438,23 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
 
 // Shared-prime pairs too big for a warp: one CTA per pair, from the
 // descriptor the warp kernel left in the big queue (so every thread builds
-// list entries at once); events are handled by the lane that raised them.
+// list entries at once); each warp takes every fourth round of 32 (alpha,
+// beta) pairs and drains its events through a warp queue as merged_kernel.
 __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const DeviceCache cache, const LaunchBuffers buf) {
+    constexpr uint32_t kWarps = kMergedThreads / 32;
     __shared__ PairDesc D;
     __shared__ __align__(16) AlphaHot s_list[kMergedListCap];
-    extern __shared__ __align__(16) uint8_t s_tab[];  // kTable2Bytes, dynamic: the wide table copy
-    for (uint32_t i = threadIdx.x; i < kTable2Bytes; i += kMergedThreads) s_tab[i] = buf.tables[kTableBytes + i];
     __shared__ uint32_t s_qi;
+    // dynamic: warp queues, root requests, then the compact tables
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_dyn);
+    RootReq* s_req = reinterpret_cast<RootReq*>(s_queue + kWarps * kQueue);
+    uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kWarps * 32 * kReqPerLane);
+    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kMergedThreads) s_tab[i] = buf.tables[i];
+    const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
+    uint64_t* q = s_queue + warp * kQueue;
+    RootReq* wreq = s_req + warp * 32 * kReqPerLane;
+    uint32_t qn = 0;
     const uint32_t count = min(*buf.big_count, buf.big_cap);
     for (;;) {
         // pairs are taken from a cursor: their sizes vary by orders of magnitude
@@ -1475,16 +1485,31 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         const PairCtx c = D.ctx;
         const uint32_t l = D.l, row = D.row;
         const uint32_t total = na * nb;
-        // thread's (ka, kb) for k = threadIdx.x + j kMergedThreads, advanced incrementally
-        uint32_t ka = threadIdx.x / nb, kb = threadIdx.x - ka * nb;
+        auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
+            const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+            if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
+            const uint2 r = merged_event((uint32_t)(ev >> 40), s_list[ka], s_list[na + kb], c, ka, kb, l, row, s_tab,
+                                         kTabD, (uint32_t)cache.limit, &buf, slots);
+            acc.cand += r.x & 0xFFFFu;
+            acc.r16 += r.y;
+            return r.x >> 16;
+        };
+        auto hit = [&](uint64_t ev, uint32_t tags) {
+            const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
+            push_hits(&buf, tags, ka, kb, l, pair_m(c), row, true);
+        };
+        // lane's (ka, kb) for k = 32 warp + lane + 128 j, advanced incrementally
+        uint32_t ka = (32 * warp + lane) / nb, kb = 32 * warp + lane - ka * nb;
         const uint32_t qs = kMergedThreads / nb, rs = kMergedThreads - qs * nb;
-        for (uint32_t k = threadIdx.x; k < total; k += kMergedThreads) {
-            const AlphaHot a = s_list[ka], bh = s_list[na + kb];
-            const uint32_t flags =
-                pair_dual(c) ? eval_fast<1, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
-                             : eval_fast<0, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
-            if (flags)
-                add_event(acc, merged_event(flags, a, bh, c, ka, kb, l, row, s_tab, kTabD2, (uint32_t)cache.limit, &buf));
+        const bool dual = pair_dual(c);
+        for (uint32_t base = 32 * warp; base < total; base += kMergedThreads) {
+            uint32_t flags = 0;
+            if (base + lane < total) {
+                const AlphaHot a = s_list[ka], bh = s_list[na + kb];
+                flags = dual ? eval_fast<1>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc)
+                             : eval_fast<0>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc);
+            }
+            if (queue_push(q, qn, flags != 0, make_event(kb, ka, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
             ka += qs;
             kb += rs;
             if (kb >= nb) {
@@ -1492,6 +1517,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
                 ++ka;
             }
         }
+        while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
         flush_acc(acc, &buf.rows[row], true);
     }
 }
@@ -1709,10 +1735,12 @@ cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const Launch
     merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    const size_t big_smem = (kMergedThreads / 32) * (kQueue * sizeof(uint64_t) + 32 * kReqPerLane * sizeof(RootReq)) +
+                            kTableBytes;
     e = cudaFuncSetAttribute((const void*)merged_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kTable2Bytes);
+                             (int)big_smem);
     if (e != cudaSuccess) return e;
-    merged_big_kernel<<<ctas, kMergedThreads, kTable2Bytes, stream>>>(cache, buf);
+    merged_big_kernel<<<ctas, kMergedThreads, big_smem, stream>>>(cache, buf);
     return cudaGetLastError();
 }
 
