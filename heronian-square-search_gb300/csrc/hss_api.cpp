@@ -40,6 +40,7 @@ constexpr uint32_t kTileCap = 16384;           // largest m-range of one item
 constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
 constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
+constexpr uint32_t kDescChunk = 1u << 22;       // shared-prime pairs set up per chunk (192 bytes each: 768 MB)
 
 
 }  // namespace
@@ -215,6 +216,9 @@ LaunchBuffers buffers(const hss_t* h, size_t row_offset) {
     b.big_count = h->d_ctrl + 4;
     b.big_next = h->d_ctrl + 6;
     b.big_cap = h->big_cap;
+    b.pair_desc = h->d_desc;
+    b.desc_chunk = h->desc_chunk;
+    b.desc_next = h->d_ctrl + 7;
     return b;
 }
 
@@ -369,6 +373,8 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     int per_sm = batched_max_ctas_per_sm(cfg.threads, cfg.min_blocks, smem);
     cfg.ctas = h->sm_count * per_sm;
     LaunchBuffers b = buffers(h, 0);
+    uint64_t pair_bound = 0;  // sets how many shared-prime chunks are launched
+    for (size_t i = 0; i < nrows; ++i) pair_bound += merged_bound(h, rows[i].l);
     std::array<cudaEvent_t, 3> ev;
     if (int e = take_events(h, &ev)) return e;
     // the group's stream work: items H2D, queue resets, the three kernels.
@@ -383,7 +389,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[0], h->stream, rec));
         HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[1], h->stream, rec));
-        HSS_CUDA(h, launch_merged(h->dev, 0, b, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, pair_bound, b, h->sm_count * 4, h->stream));
         HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[2], h->stream, rec));
         return HSS_OK;
@@ -440,7 +446,7 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
         HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
         HSS_CUDA(h, launch_plain(h->dev, b, nrows, acap, buf, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
-        HSS_CUDA(h, launch_merged(h->dev, 0, buf, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, bound, buf, h->sm_count * 4, h->stream));
         HSS_CUDA(h, launch_exact(h->dev, buf, h->sm_count * 4, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
         h->marks.push_back(ev);
@@ -632,10 +638,12 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
     h->merged_cap = (uint32_t)kMergedCap;
     h->big_cap = 1u << 20;
+    h->desc_chunk = kDescChunk;
     h->exact_cap = 1u << 24;
     if ((s = upload(h, &h->d_tables, tables.data(), kTableTotalBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
         (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
-        (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
+        (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) ||
+        (s = device_alloc(h, &h->d_desc, (size_t)h->desc_chunk * kBigEntryWords)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
         (s = ensure_rows(h, 1024))) {
         hss_close(h);
         return s;

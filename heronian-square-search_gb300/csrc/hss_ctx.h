@@ -41,9 +41,11 @@ struct hss_ctx {
     size_t rows_cap = 0;
     hss::DevHit* d_hits = nullptr;
     uint32_t hit_cap = 0;
-    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count [5] exact_count [6] big_next
+    unsigned int* d_ctrl = nullptr;  // [0] hit_count [1] merged_count [2] next_item [3] error flags [4] big_count [5] exact_count [6] big_next [7] desc_next
     uint4* d_big = nullptr;          // shared-prime pairs too big for a warp
     uint32_t big_cap = 0;
+    uint4* d_desc = nullptr;         // descriptors of one chunk of shared-prime pairs
+    uint32_t desc_chunk = 0;
     hss::ExactItem* d_exact = nullptr;    // exact work queue
     uint32_t exact_cap = 0;
     bool exact_overflow = false;          // the last launch group outgrew it

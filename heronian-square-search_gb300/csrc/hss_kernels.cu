@@ -34,9 +34,11 @@
 // items from a global cursor; per item the row's values are staged in shared
 // memory, and each warp walks the m-side records of 128 roots (read from the
 // cache, coalesced) in lockstep rounds against them.  plain_kernel keeps the reference's shape
-// (a block per (row, slice), one thread per pair).  merged_kernel (a warp per
-// pair) and merged_big_kernel (a CTA per pair) handle the pairs that share a
-// split prime (gpu_search_v42.cu:318-341).
+// (a block per (row, slice), one thread per pair).  The pairs that share a
+// split prime (gpu_search_v42.cu:318-341) are set up by merged_setup_kernel (a
+// thread per pair, in chunks of the queue) and run by merged_kernel (a warp
+// per pair) or, when their lists exceed a warp's slice, merged_big_kernel (a
+// CTA per pair).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
@@ -1174,7 +1176,7 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
     S.ok = 1;
     uint32_t mp[9], me[9], nm = 0;
     i128 fixed = (i128)2 * (i128)R.fixed;
-    uint64_t x = m;
+    uint32_t x = (uint32_t)m;  // m <= 3e7: 32-bit divisions
     while (x > 1) {
         uint32_t p = cache.spf[x], a = 0;
         do {
@@ -1325,58 +1327,81 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
     out.ia = ri;
 }
 
-// Shared-prime pairs, a warp per pair, 32 pairs set up at once: each lane
-// factors one pair's m, splits its terms and computes its pair constants into
-// the warp's descriptor slots; then the warp takes the 32 pairs in turn,
-// builds both lists in its shared slice (float and residue products of the
-// prime-power values) and evaluates all (alpha, beta) combinations in lockstep
-// rounds of 32 with a warp event queue.  Pairs whose lists exceed the slice go
-// to the big-pair queue (one CTA per pair).
+// Shared-prime pair set-up, one thread per pair of one chunk of the queue
+// (entries chunk0 .. chunk0 + desc_chunk - 1): factors m, splits the pair's
+// terms and computes its constants into the pair's descriptor slot.  Pairs
+// whose lists exceed a warp's slice also go to the big-pair queue (one CTA
+// per pair).  Kept apart from the warp kernel, whose filter loop then has the
+// instruction cache to itself.
+__global__ void __launch_bounds__(128) merged_setup_kernel(const DeviceCache cache, const LaunchBuffers buf,
+                                                         uint32_t chunk0) {
+    const uint32_t count = min(*buf.merged_count, buf.merged_cap);
+    if (chunk0 >= count) return;
+    const uint32_t n = min(count - chunk0, buf.desc_chunk);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 e = buf.merged_queue[chunk0 + i];
+        PairDesc D;
+        pair_desc_setup(cache, buf.row_info[e.z], e, D, kWarpListCap);
+        const uint4* src = reinterpret_cast<const uint4*>(&D);
+        if (D.state == 2) {
+            unsigned int idx = atomicAdd(buf.big_count, 1u);
+            if (idx < buf.big_cap) {
+                uint4* dst = buf.big_queue + (size_t)idx * kBigEntryWords;
+                for (uint32_t w = 0; w < sizeof(PairDesc) / 16; ++w) dst[w] = src[w];
+            } else {
+                atomicOr(buf.error_flags, 2u);
+            }
+        } else if (D.state == 3) {
+            atomicOr(buf.error_flags, 2u);
+        }
+        uint4* dst = buf.pair_desc + (size_t)i * kBigEntryWords;
+        for (uint32_t w = 0; w < sizeof(PairDesc) / 16; ++w) dst[w] = src[w];
+    }
+}
+
+// Shared-prime pairs of one chunk, a warp per pair, 32 consecutive pairs per
+// warp at a time: the warp reads the pair's descriptor (the next one is
+// loaded while the current pair runs), builds both lists in its shared slice
+// (float and residue products of the prime-power values) and evaluates all
+// (alpha, beta) combinations in lockstep rounds of 32 with a warp event queue.
 constexpr uint32_t kPairWarps = 4;
-__global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf) {
-    __shared__ __align__(16) PairDesc s_desc[kPairWarps][32];
+__global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf,
+                                                                  uint32_t chunk0) {
+    __shared__ __align__(16) PairDesc s_desc[kPairWarps];
     __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
     __shared__ uint64_t s_queue[kPairWarps][kQueue];
-    // dynamic (static use is near 48 KB): root requests, then the tables
+    // dynamic: root requests, then the wide tables
     extern __shared__ __align__(16) unsigned char s_dyn[];
     RootReq* s_req = reinterpret_cast<RootReq*>(s_dyn);
     uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kPairWarps * 32 * kReqPerLane);
-    for (uint32_t i = threadIdx.x; i < kTableBytes; i += kPairWarps * 32) s_tab[i] = buf.tables[i];
+    const uint32_t count = min(*buf.merged_count, buf.merged_cap);
+    if (chunk0 >= count) return;
+    const uint32_t n = min(count - chunk0, buf.desc_chunk);
+    for (uint32_t i = threadIdx.x; i < kTable2Bytes; i += kPairWarps * 32) s_tab[i] = buf.tables[kTableBytes + i];
     __syncthreads();
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
-    PairDesc* desc = s_desc[warp];
+    PairDesc& D = s_desc[warp];
+    uint4* dwords = reinterpret_cast<uint4*>(&D);
+    constexpr uint32_t kDescWords = sizeof(PairDesc) / 16;
     AlphaHot* list = s_list[warp];
     uint64_t* q = s_queue[warp];
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
-    const uint32_t count = min(*buf.merged_count, buf.merged_cap);
-    const uint32_t stride = gridDim.x * kPairWarps * 32;
-    for (uint32_t b0 = (blockIdx.x * kPairWarps + warp) * 32; b0 < count; b0 += stride) {
-        const uint32_t qi = b0 + lane;
-        if (qi < count) {
-            const uint4 e = buf.merged_queue[qi];
-            pair_desc_setup(cache, buf.row_info[e.z], e, desc[lane], kWarpListCap);
-            if (desc[lane].state == 2) {
-                // the descriptor goes with the pair: the big kernel sets nothing up
-                unsigned int idx = atomicAdd(buf.big_count, 1u);
-                if (idx < buf.big_cap) {
-                    const uint4* src = reinterpret_cast<const uint4*>(&desc[lane]);
-                    uint4* dst = buf.big_queue + (size_t)idx * kBigEntryWords;
-                    for (uint32_t w = 0; w < sizeof(PairDesc) / 16; ++w) dst[w] = src[w];
-                } else {
-                    atomicOr(buf.error_flags, 2u);
-                }
-            } else if (desc[lane].state == 3) {
-                atomicOr(buf.error_flags, 2u);
-            }
-        } else {
-            desc[lane].state = 0;
-        }
-        __syncwarp();
+    // blocks of 32 consecutive pairs from the chunk's cursor (pair sizes vary widely)
+    for (;;) {
+        uint32_t b0 = 0;
+        if (lane == 0) b0 = atomicAdd(buf.desc_next, 32u);
+        b0 = __shfl_sync(kFull, b0, 0);
+        if (b0 >= n) break;
+        const uint32_t b1 = min(b0 + 32, n);
+        uint4 next = lane < kDescWords ? buf.pair_desc[(size_t)b0 * kBigEntryWords + lane] : make_uint4(0, 0, 0, 0);
         Acc acc{0, 0, 0, 0, 0, 0};
         uint32_t cur_row = 0xFFFFFFFFu;
-        for (uint32_t i = 0; i < 32; ++i) {
-            const PairDesc& D = desc[i];
+        for (uint32_t i = b0; i < b1; ++i) {
+            __syncwarp();
+            if (lane < kDescWords) dwords[lane] = next;
+            if (i + 1 < b1 && lane < kDescWords) next = buf.pair_desc[(size_t)(i + 1) * kBigEntryWords + lane];
+            __syncwarp();
             if (D.state != 1) continue;
             if (D.row != cur_row) {
                 if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
@@ -1403,7 +1428,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                 const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
                 if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
                 const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], list[na + kb], c, ka, kb, l, row, s_tab,
-                                             kTabD, (uint32_t)cache.limit, &buf, slots);
+                                             kTabD2, (uint32_t)cache.limit, &buf, slots);
                 acc.cand += r.x & 0xFFFFu;
                 acc.r16 += r.y;
                 return r.x >> 16;
@@ -1417,7 +1442,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
                 uint32_t flags = 0;
                 if (base + lane < total) {
                     const AlphaHot a = list[ka], bh = list[na + kb];
-                    flags = eval_fast<2>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc, dual);
+                    flags = eval_fast<2, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc, dual);
                 }
                 if (queue_push(q, qn, flags != 0, make_event(kb, ka, flags)))
                     drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
@@ -1725,16 +1750,27 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
     return cudaGetLastError();
 }
 
-cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf, int ctas,
+cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const LaunchBuffers& buf, int ctas,
                           cudaStream_t stream) {
-    (void)count;
-    const size_t smem = kPairWarps * 32 * kReqPerLane * sizeof(RootReq) + kTableBytes;
+    const size_t smem = kPairWarps * 32 * kReqPerLane * sizeof(RootReq) + kTable2Bytes;
     cudaError_t e = cudaFuncSetAttribute((const void*)merged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    // chunks of the queue: set-up, then the warp kernel; launches past the
+    // queue's actual length return at once
+    const uint64_t pairs = pair_bound < buf.merged_cap ? pair_bound : buf.merged_cap;
+    for (uint64_t c0 = 0; c0 < pairs; c0 += buf.desc_chunk) {
+        const uint32_t n = (uint32_t)(pairs - c0 < buf.desc_chunk ? pairs - c0 : buf.desc_chunk);
+        const int setup_ctas = (int)((n + 127) / 128 < (uint64_t)ctas * 4 ? (n + 127) / 128 : (uint64_t)ctas * 4);
+        merged_setup_kernel<<<setup_ctas, 128, 0, stream>>>(cache, buf, (uint32_t)c0);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(buf.desc_next, 0, sizeof(unsigned int), stream);
+        if (e != cudaSuccess) return e;
+        merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf, (uint32_t)c0);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     const size_t big_smem = (kMergedThreads / 32) * (kQueue * sizeof(uint64_t) + 32 * kReqPerLane * sizeof(RootReq)) +
                             kTableBytes;
     e = cudaFuncSetAttribute((const void*)merged_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -72,6 +72,10 @@ struct LaunchBuffers {
     unsigned int* big_count;
     unsigned int* big_next;     // cursor of the big-pair kernel over big_queue
     uint32_t big_cap;
+    uint4* pair_desc;           // descriptors of one chunk of the shared-prime queue
+                                // (kBigEntryWords words each), set up for the warp kernel
+    uint32_t desc_chunk;        // pairs per chunk
+    unsigned int* desc_next;    // cursor of the warp kernel over the chunk (blocks of 32 pairs)
     const uint8_t* tables;      // kTableTotalBytes residue tables (compact, then wide)
     const RowInfo* row_info;    // [n_rows] constants of the launch's rows
     ExactItem* exact_queue;     // rare exact work (undecided products, possible hits)
@@ -107,8 +111,11 @@ cudaError_t launch_batched(const DeviceCache& cache, const WorkItem* items, uint
 cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_rows,
                          uint32_t alpha_cap, const LaunchBuffers& buf, cudaStream_t stream);
 
-// Pairs sharing a split prime, read from buf.merged_queue[0 .. count).
-cudaError_t launch_merged(const DeviceCache& cache, uint32_t count, const LaunchBuffers& buf,
+// Pairs sharing a split prime, read from buf.merged_queue (as many as the
+// kernels before appended; pair_bound: an upper bound on that number, which
+// sets how many chunks of buf.desc_chunk pairs are launched), then the big
+// pairs they left in buf.big_queue.
+cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const LaunchBuffers& buf,
                           int ctas, cudaStream_t stream);
 
 // Integer-op throughput of the device measured by a probe kernel (ops/s).

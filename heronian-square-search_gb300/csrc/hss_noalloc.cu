@@ -38,6 +38,7 @@ constexpr uint32_t kNaRows = 64;          // root rows per call
 constexpr uint32_t kNaItems = 8192;       // work items per call
 constexpr uint32_t kNaMerged = 1u << 20;  // pairs sharing a split prime per call
 constexpr uint32_t kNaBig = 1u << 13;     // of which too big for one warp
+constexpr uint32_t kNaDesc = 1u << 14;    // shared-prime pairs set up per chunk
 constexpr uint32_t kNaExact = 1u << 16;   // exact work items per call
 constexpr uint32_t kNaHits = 4096;        // hits kept per call (as the reference, gpu_search_v42.cu:177-178)
 constexpr uint32_t kNaCtrl = 8;
@@ -50,7 +51,8 @@ constexpr size_t kOffHits = align256(kOffRowInfo + kNaRows * sizeof(RowInfo));
 constexpr size_t kOffItems = align256(kOffHits + kNaHits * sizeof(DevHit));
 constexpr size_t kOffMerged = align256(kOffItems + kNaItems * sizeof(WorkItem));
 constexpr size_t kOffBig = align256(kOffMerged + (size_t)kNaMerged * sizeof(uint4));
-constexpr size_t kOffExact = align256(kOffBig + (size_t)kNaBig * kBigEntryWords * sizeof(uint4));
+constexpr size_t kOffDesc = align256(kOffBig + (size_t)kNaBig * kBigEntryWords * sizeof(uint4));
+constexpr size_t kOffExact = align256(kOffDesc + (size_t)kNaDesc * kBigEntryWords * sizeof(uint4));
 constexpr size_t kNoAllocBytes = align256(kOffExact + kNaExact * sizeof(ExactItem));
 static_assert(kNoAllocBytes <= (24u << 20), "scratch stays within 24 MiB");
 
@@ -161,6 +163,9 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     b.big_count = ctrl + 4;
     b.big_next = ctrl + 6;
     b.big_cap = kNaBig;
+    b.pair_desc = reinterpret_cast<uint4*>(base + kOffDesc);
+    b.desc_chunk = kNaDesc;
+    b.desc_next = ctrl + 7;
     b.exact_queue = reinterpret_cast<ExactItem*>(base + kOffExact);
     b.exact_count = ctrl + 5;
     b.exact_cap = kNaExact;
@@ -181,7 +186,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
                                                      batched_smem_bytes(cfg.threads, alpha_cap));
     NA_CUDA(cudaEventRecord(h->ev0, st));
     NA_CUDA(launch_batched(h->dev, reinterpret_cast<const WorkItem*>(base + kOffItems), n_items, cfg, b, st));
-    NA_CUDA(launch_merged(h->dev, 0, b, h->sm_count * 4, st));
+    NA_CUDA(launch_merged(h->dev, shared, b, h->sm_count * 4, st));
     NA_CUDA(launch_exact(h->dev, b, h->sm_count * 4, st));
     NA_CUDA(cudaEventRecord(h->ev1, st));
     NA_CUDA(cudaMemcpyAsync(g_host_ctrl, ctrl, sizeof g_host_ctrl, cudaMemcpyDeviceToHost, st));

@@ -164,7 +164,7 @@ int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tu
  * by a pool or an embedding runtime fixed at start-up, or loops that cannot
  * take the synchronisation an allocation implies.  hss_search grows its
  * per-call buffers with cudaMalloc / cudaMallocHost; this call allocates
- * nothing: its device scratch is one array of about 19 MiB that is static in
+ * nothing: its device scratch is one array of about 23 MiB that is static in
  * the library (every GPU that loads the library holds it until the process
  * exits), its host staging is static too, and the handle's cache, stream and
  * tables (made by hss_open) are the inputs.  Limits per call: at most 64 root
