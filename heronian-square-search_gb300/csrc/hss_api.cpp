@@ -381,6 +381,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     // Inside a capture the timing events become event-record nodes
     // (cudaEventRecordExternal), so they still time the graph's kernels.
     const unsigned int rec = h->opts.use_graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+    uint32_t merged_launches = 0;
     auto enqueue = [&]() -> int {
         HSS_CUDA(h, cudaMemcpyAsync(h->d_items, h->h_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice,
                                     h->stream));
@@ -389,7 +390,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[0], h->stream, rec));
         HSS_CUDA(h, launch_batched(h->dev, h->d_items, (uint32_t)n_items, cfg, b, h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[1], h->stream, rec));
-        HSS_CUDA(h, launch_merged(h->dev, pair_bound, b, h->sm_count * 4, h->stream));
+        HSS_CUDA(h, launch_merged(h->dev, pair_bound, b, h->sm_count * 4, h->stream, &merged_launches));
         HSS_CUDA(h, launch_exact(h->dev, b, h->sm_count * 4, h->stream));
         HSS_CUDA(h, cudaEventRecordWithFlags(ev[2], h->stream, rec));
         return HSS_OK;
@@ -401,7 +402,7 @@ int run_batched_rows(hss_t* h, const RowRef* rows, size_t nrows) {
     }
     h->h2d_bytes += n_items * sizeof(WorkItem);
     h->marks.push_back(ev);
-    h->launches += 4;
+    h->launches += 2 + merged_launches;  // batched, shared-prime kernels, exact
     return HSS_OK;
 }
 
@@ -446,11 +447,12 @@ int run_plain(hss_t* h, uint64_t first, uint64_t last) {
         HSS_CUDA(h, cudaEventRecord(ev[0], h->stream));
         HSS_CUDA(h, launch_plain(h->dev, b, nrows, acap, buf, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[1], h->stream));
-        HSS_CUDA(h, launch_merged(h->dev, bound, buf, h->sm_count * 4, h->stream));
+        uint32_t merged_launches = 0;
+        HSS_CUDA(h, launch_merged(h->dev, bound, buf, h->sm_count * 4, h->stream, &merged_launches));
         HSS_CUDA(h, launch_exact(h->dev, buf, h->sm_count * 4, h->stream));
         HSS_CUDA(h, cudaEventRecord(ev[2], h->stream));
         h->marks.push_back(ev);
-        h->launches += 4;
+        h->launches += 2 + merged_launches;  // plain, shared-prime kernels, exact
     }
     return HSS_OK;
 }

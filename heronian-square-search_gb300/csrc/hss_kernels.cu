@@ -1751,7 +1751,8 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 }
 
 cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const LaunchBuffers& buf, int ctas,
-                          cudaStream_t stream) {
+                          cudaStream_t stream, uint32_t* launches) {
+    *launches = 0;
     const size_t smem = kPairWarps * 32 * kReqPerLane * sizeof(RootReq) + kTable2Bytes;
     cudaError_t e = cudaFuncSetAttribute((const void*)merged_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
@@ -1770,6 +1771,7 @@ cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const L
         merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf, (uint32_t)c0);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        *launches += 2;
     }
     const size_t big_smem = (kMergedThreads / 32) * (kQueue * sizeof(uint64_t) + 32 * kReqPerLane * sizeof(RootReq)) +
                             kTableBytes;
@@ -1777,6 +1779,7 @@ cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const L
                              (int)big_smem);
     if (e != cudaSuccess) return e;
     merged_big_kernel<<<ctas, kMergedThreads, big_smem, stream>>>(cache, buf);
+    *launches += 1;
     return cudaGetLastError();
 }
 

@@ -114,9 +114,10 @@ cudaError_t launch_plain(const DeviceCache& cache, uint64_t first_l, uint32_t n_
 // Pairs sharing a split prime, read from buf.merged_queue (as many as the
 // kernels before appended; pair_bound: an upper bound on that number, which
 // sets how many chunks of buf.desc_chunk pairs are launched), then the big
-// pairs they left in buf.big_queue.
+// pairs they left in buf.big_queue.  *launches receives the number of
+// kernels launched.
 cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const LaunchBuffers& buf,
-                          int ctas, cudaStream_t stream);
+                          int ctas, cudaStream_t stream, uint32_t* launches);
 
 // Integer-op throughput of the device measured by a probe kernel (ops/s).
 double int32_peak_ops(int device, int sm_count, double* ms);

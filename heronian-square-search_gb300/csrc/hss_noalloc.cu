@@ -186,7 +186,8 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
                                                      batched_smem_bytes(cfg.threads, alpha_cap));
     NA_CUDA(cudaEventRecord(h->ev0, st));
     NA_CUDA(launch_batched(h->dev, reinterpret_cast<const WorkItem*>(base + kOffItems), n_items, cfg, b, st));
-    NA_CUDA(launch_merged(h->dev, shared, b, h->sm_count * 4, st));
+    uint32_t merged_launches = 0;
+    NA_CUDA(launch_merged(h->dev, shared, b, h->sm_count * 4, st, &merged_launches));
     NA_CUDA(launch_exact(h->dev, b, h->sm_count * 4, st));
     NA_CUDA(cudaEventRecord(h->ev1, st));
     NA_CUDA(cudaMemcpyAsync(g_host_ctrl, ctrl, sizeof g_host_ctrl, cudaMemcpyDeviceToHost, st));
@@ -225,7 +226,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     const uint32_t found = g_host_ctrl[0] > kNaHits ? g_host_ctrl[0] : unique;
     out->hits = found;
     out->kernel_ms = ms;
-    out->launches = 4;
+    out->launches = 2 + merged_launches;
     out->h2d_bytes = rows * sizeof(RowInfo) + n_items * sizeof(WorkItem);
     out->d2h_bytes = sizeof g_host_ctrl + rows * sizeof(RowCounts) + nh * sizeof(DevHit);
     for (uint32_t i = 0; i < unique && i < hit_cap && hits; ++i) {
