@@ -435,28 +435,84 @@ __device__ __forceinline__ bool root_match(uint32_t n, uint32_t zres) {
            pow4_mod(n % kModD, kModD) == ((zres >> kShiftD) & kMaskD);
 }
 
+// First n >= nlo with the parity of z (n^4 = z mod 2 forces n = z mod 2;
+// bit 0 of zres is z mod 2, as 2 divides 9360): only every second n of a
+// window can be a root.
+__device__ __forceinline__ uint32_t root_first(uint32_t nlo, uint32_t zres) { return nlo + ((nlo ^ zres) & 1u); }
+
 // One thread scans the window (paths without a warp queue).
 __device__ bool root_scan(uint32_t nlo, uint32_t nhi, uint32_t zres) {
-    for (uint32_t n = nlo; n <= nhi; ++n)
+    for (uint32_t n = root_first(nlo, zres); n <= nhi; n += 2)
         if (root_match(n, zres)) return true;
     return false;
 }
 
 // A root-filter request left by an event for its warp: the window and packed
 // residues of one counted term, and the orientation (tag = 2p + o) whose
-// exact hit test it gates.  The warp scans each request together, one n per
-// lane, instead of one lane walking the window while the others wait.
+// exact hit test it gates.  The warp scans the requests of all its lanes
+// together: their candidate roots (every second n of each window) are laid
+// end to end and taken 32 at a time, one per lane, instead of one lane
+// walking a window while the others wait.
 struct RootReq {
     uint32_t nlo, nhi, zres, tag;
 };
 constexpr uint32_t kReqPerLane = 2;  // per event; further terms are scanned by the lane itself
 
-__device__ __forceinline__ bool root_scan_warp(const RootReq& rq, uint32_t lane) {
-    for (uint32_t base = rq.nlo; base <= rq.nhi; base += 32) {
-        const uint32_t n = base + lane;
-        if (__any_sync(kFull, n <= rq.nhi && root_match(n, rq.zres))) return true;
+// Number of candidate roots of a request.
+__device__ __forceinline__ uint32_t root_count(const RootReq& rq) {
+    const uint32_t n0 = root_first(rq.nlo, rq.zres);
+    return n0 <= rq.nhi ? (rq.nhi - n0) / 2 + 1 : 0u;
+}
+
+// Scans the requests wreq[lane * kReqPerLane + r], r < cnt (cnt per lane,
+// at most kReqPerLane); returns, per lane, the tags of its requests whose
+// window holds an n with n^4 = z in both residue fields.  All 32 lanes call it.
+__device__ __forceinline__ uint32_t root_scan_requests(const RootReq* wreq, uint32_t cnt, uint32_t lane) {
+    uint32_t num0 = 0, mine = 0;
+#pragma unroll
+    for (uint32_t r = 0; r < kReqPerLane; ++r) {
+        const uint32_t c = r < cnt ? root_count(wreq[lane * kReqPerLane + r]) : 0u;
+        if (r == 0) num0 = c;
+        mine += c;
     }
-    return false;
+    uint32_t incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, incl, d);
+        if (lane >= (uint32_t)d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31), excl = incl - mine;
+    uint32_t passed = 0;
+    for (uint32_t base = 0; base < total; base += 32) {
+        const uint32_t s = base + lane;
+        // owning lane of candidate s: the first lane whose inclusive sum exceeds s
+        uint32_t owner = 0;
+#pragma unroll
+        for (uint32_t step = 16; step >= 1; step >>= 1) {
+            const uint32_t v = __shfl_sync(kFull, incl, owner + step - 1);
+            if (v <= s) owner += step;
+        }
+        owner &= 31u;
+        uint32_t off = s - __shfl_sync(kFull, excl, owner);
+        const uint32_t n0 = __shfl_sync(kFull, num0, owner);
+        const uint32_t r = off < n0 ? 0u : 1u;
+        off -= r ? n0 : 0u;
+        bool match = false;
+        uint32_t tag = 0;
+        if (s < total) {
+            const RootReq rq = wreq[owner * kReqPerLane + r];
+            tag = rq.tag;
+            match = root_match(root_first(rq.nlo, rq.zres) + 2u * off, rq.zres);
+        }
+        uint32_t mm = __ballot_sync(kFull, match);
+        while (mm) {  // rare: a possible root
+            const uint32_t src = __ffs(mm) - 1;
+            mm &= mm - 1;
+            const uint32_t o = __shfl_sync(kFull, owner, src), t = __shfl_sync(kFull, tag, src);
+            if (lane == o) passed |= 1u << t;
+        }
+    }
+    return passed;
 }
 
 // Exact coordinates for the rare exact path.
@@ -814,22 +870,14 @@ __device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, 
         info = handle(ev, wreq + lane * kReqPerLane);
     }
     __syncwarp();
-    const uint32_t nreq = info & 15u;
+    uint32_t nreq = info & 15u;
     uint32_t passed = (info >> 4) & 15u;
-    uint32_t todo = __ballot_sync(kFull, nreq != 0);
-    while (todo) {
-        const uint32_t src = __ffs(todo) - 1;
-        todo &= todo - 1;
-        uint32_t cnt = __shfl_sync(kFull, nreq, src);
-        if (cnt > kReqPerLane) {
-            if (lane == 0) atomicOr(err, kErrIndex);
-            cnt = kReqPerLane;
-        }
-        for (uint32_t r = 0; r < cnt; ++r) {
-            const RootReq rq = wreq[src * kReqPerLane + r];
-            if (root_scan_warp(rq, lane) && lane == src) passed |= 1u << rq.tag;
-        }
+    if (nreq > kReqPerLane) {
+        atomicOr(err, kErrIndex);
+        nreq = kReqPerLane;
     }
+    __syncwarp();
+    if (__any_sync(kFull, nreq != 0)) passed |= root_scan_requests(wreq, nreq, lane);
     if (passed) hit(ev, passed);
     __syncwarp();
     const uint32_t rest = count - n;
