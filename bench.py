@@ -332,6 +332,11 @@ def our_arm(args, rank, world, local_rank):
         return 0
     plain = s.search(first, last, mode="plain") if not args.no_plain else None
     serve = serving(s) if not args.no_serving else None
+    # the same cache built by host threads and uploaded (the other way to open)
+    t0 = time.time()
+    with hss.Search(LIMIT, device=local_rank, host_build=1) as hb:
+        host_open_s = time.time() - t0
+        host_info = hb.info()
     # integer roofline of the persistent kernel
     import ctypes
     lib = hss.load_library()
@@ -390,7 +395,9 @@ def our_arm(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "gpu_launches": sum(r.counts["launches"] for r, _ in steps),
         "clocks": clocks,
-        "prep": {"open_seconds": open_s, "host_cache_seconds": info["prep_seconds"], "records": info["records"]},
+        "prep": {"open_seconds": open_s, "device_cache_seconds": info["prep_seconds"], "records": info["records"],
+                 "host_build_open_seconds": host_open_s, "host_cache_seconds": host_info["prep_seconds"],
+                 "host_build_records_equal": host_info["records"] == info["records"]},
     }
     print(json.dumps(line))
     s.close()

@@ -567,6 +567,59 @@ const char* hss_strerror(int status) {
 
 const char* hss_last_error(const hss_t* h) { return h ? h->err.c_str() : "null handle"; }
 
+int hss_cache_check(uint64_t limit, int device, uint64_t* mismatches, double* host_seconds,
+                    double* device_seconds) {
+    if (!mismatches || limit < 1 || limit > HSS_MAX_LIMIT) return HSS_ERR_ARGUMENT;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || cudaSetDevice(device) != cudaSuccess)
+        return HSS_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return HSS_ERR_NO_DEVICE;
+    HostCache hc;
+    std::string err;
+    unsigned hw = std::thread::hardware_concurrency();
+    int s = build_host_cache(limit, (int)(hw ? hw : 1), &hc, &err);
+    if (s) return s;
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return HSS_ERR_CUDA;
+    DeviceBuild db;
+    s = build_device_cache(limit, prop.multiProcessorCount, st, &db, &err);
+    cudaStreamDestroy(st);
+    if (s) return s;
+    uint64_t bad = 0;
+    auto compare = [&](const void* dev, const void* host, size_t count, size_t elem) -> int {
+        std::vector<unsigned char> copy(count * elem);
+        if (count && cudaMemcpy(copy.data(), dev, count * elem, cudaMemcpyDeviceToHost) != cudaSuccess)
+            return HSS_ERR_CUDA;
+        const unsigned char* h = static_cast<const unsigned char*>(host);
+        for (size_t i = 0; i < count; ++i)
+            if (memcmp(copy.data() + i * elem, h + i * elem, elem) != 0) ++bad;
+        return HSS_OK;
+    };
+    bad += (db.records != hc.records) + (db.pp_count != hc.pp_hot.size()) +
+           (db.reference_flattened != hc.reference_flattened) + (db.reference_cached != hc.reference_cached) +
+           (db.max_exponent != hc.max_exponent);
+    if (!bad) {
+        if ((s = compare(db.spf, hc.spf.data(), hc.spf.size(), sizeof(uint32_t))) ||
+            (s = compare(db.seg_off, hc.seg_off.data(), hc.seg_off.size(), sizeof(uint32_t))) ||
+            (s = compare(db.hot, hc.hot.get(), hc.records, sizeof(HotRec))) ||
+            (s = compare(db.exact, hc.exact.get(), hc.records, sizeof(ExactRec))) ||
+            (s = compare(db.owner, hc.owner.get(), hc.records, sizeof(uint32_t))) ||
+            (s = compare(db.pp_base, hc.pp_base.data(), hc.pp_base.size(), sizeof(uint32_t))) ||
+            (s = compare(db.pp_hot, hc.pp_hot.data(), hc.pp_hot.size(), sizeof(HotRec))) ||
+            (s = compare(db.pp_exact, hc.pp_exact.data(), hc.pp_exact.size(), sizeof(__int128)))) {
+            for (void* p : db.owned) cudaFree(p);
+            return s;
+        }
+        bad += (db.spf_host != hc.spf) + (db.seg_off_host != hc.seg_off);
+    }
+    for (void* p : db.owned) cudaFree(p);
+    *mismatches = bad;
+    if (host_seconds) *host_seconds = hc.seconds;
+    if (device_seconds) *device_seconds = db.seconds;
+    return HSS_OK;
+}
+
 int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     if (!out) return HSS_ERR_ARGUMENT;
     *out = nullptr;
@@ -588,7 +641,41 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     }
     h->sm_count = prop.multiProcessorCount;
     int s = HSS_OK;
-    {
+    if (!h->opts.host_build) {
+        // the cache built by kernels on the device (same arrays and values as the host build)
+        if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete h;
+            return HSS_ERR_CUDA;
+        }
+        DeviceBuild db;
+        std::string err;
+        s = build_device_cache(limit, h->sm_count, h->stream, &db, &err);
+        if (s) {
+            hss_close(h);
+            return s;
+        }
+        h->allocations.insert(h->allocations.end(), db.owned.begin(), db.owned.end());
+        if (db.longest > kItemRecords) {
+            hss_close(h);
+            return HSS_ERR_LIMIT;
+        }
+        h->records = db.records;
+        h->ref_flattened = db.reference_flattened;
+        h->ref_cached = db.reference_cached;
+        h->prep_seconds = db.seconds;
+        h->dev.limit = limit;
+        h->dev.spf = db.spf;
+        h->dev.seg_off = db.seg_off;
+        h->dev.hot = db.hot;
+        h->dev.exact = db.exact;
+        h->dev.owner = db.owner;
+        h->dev.pp_base = db.pp_base;
+        h->dev.pp_hot = db.pp_hot;
+        h->dev.pp_exact = db.pp_exact;
+        h->dev.max_exponent = db.max_exponent;
+        h->seg_off = std::move(db.seg_off_host);
+        h->spf = std::move(db.spf_host);
+    } else {
         HostCache hc;
         std::string err;
         unsigned hw = std::thread::hardware_concurrency();
@@ -650,7 +737,7 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
         hss_close(h);
         return s;
     }
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+    if ((!h->stream && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) ||
         cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
         hss_close(h);
         return HSS_ERR_CUDA;

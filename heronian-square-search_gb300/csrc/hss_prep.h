@@ -8,6 +8,8 @@
 
 #include "hss_internal.h"
 
+struct CUstream_st;  // cudaStream_t
+
 namespace hss {
 
 // Per-integer factor summary used on the host (and by the item builder).
@@ -44,5 +46,30 @@ int build_host_cache(uint64_t limit, int threads, HostCache* out, std::string* e
 
 // Factor summary of x from the smallest-prime-factor table.
 NumberFactors factor_number(const uint32_t* spf, uint64_t x);
+
+// The same cache built on the current device (hss_devprep.cu): device arrays
+// with the host cache's layout and values, host copies of spf and seg_off.
+// `owned` lists every device allocation of the result (the caller frees them).
+struct DeviceBuild {
+    uint64_t limit = 0;
+    uint32_t* spf = nullptr;       // [N+1]
+    uint32_t* seg_off = nullptr;   // [N+2]
+    HotRec* hot = nullptr;         // [records]
+    ExactRec* exact = nullptr;     // [records]
+    uint32_t* owner = nullptr;     // [records]
+    uint32_t* pp_base = nullptr;   // [N+1]
+    HotRec* pp_hot = nullptr;      // [pp_count]
+    __int128* pp_exact = nullptr;  // [2 pp_count]
+    uint64_t records = 0, pp_count = 0;
+    uint32_t max_exponent = 0, longest = 0;  // longest: the largest segment
+    uint64_t reference_flattened = 0, reference_cached = 0;
+    std::vector<uint32_t> spf_host, seg_off_host;
+    std::vector<void*> owned;
+    double seconds = 0;
+};
+
+// Builds the cache for limit N on the current device, on `stream`, with grids
+// of sm_count * 8 CTAs.  Returns 0 or a negative hss status with *err set.
+int build_device_cache(uint64_t limit, int sm_count, CUstream_st* stream, DeviceBuild* out, std::string* err);
 
 }  // namespace hss

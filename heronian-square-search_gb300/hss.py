@@ -27,7 +27,8 @@ MODE_BATCHED = 1
 class HssOpts(ctypes.Structure):
     _fields_ = [("prep_threads", ctypes.c_uint32), ("hit_capacity", ctypes.c_uint32),
                 ("block_threads", ctypes.c_uint32), ("item_target", ctypes.c_uint32),
-                ("ctas_per_sm", ctypes.c_uint32), ("use_graph", ctypes.c_uint32)]
+                ("ctas_per_sm", ctypes.c_uint32), ("use_graph", ctypes.c_uint32),
+                ("host_build", ctypes.c_uint32)]
 
 
 class HssCounts(ctypes.Structure):
@@ -103,6 +104,7 @@ def load_library(path: Optional[os.PathLike] = None) -> ctypes.CDLL:
     lib.hss_poll.argtypes = [ctypes.c_void_p, u64, p(HssRequestInfo), p(HssHit), u32]
     lib.hss_wait.argtypes = [ctypes.c_void_p, u64, p(HssRequestInfo), p(HssHit), u32]
     lib.hss_serve_stop.argtypes = [ctypes.c_void_p]
+    lib.hss_cache_check.argtypes = [u64, i32, p(u64), p(ctypes.c_double), p(ctypes.c_double)]
     if path is None:
         _lib = lib
     return lib
@@ -141,6 +143,17 @@ def cache_inspect(limit: int, x: int = 0, cap: int = 1 << 16):
     values = [(re[i], im[i]) for i in range(min(cnt.value, cap))] if x else []
     return {"records": rec.value, "flattened": flat.value, "cached": cached.value,
             "segment": values}
+
+
+def cache_check(limit: int, device: int = 0) -> Dict[str, float]:
+    """Builds the factor cache on the host and on the device and compares every
+    array entry; returns the mismatch count and both build times."""
+    lib = load_library()
+    bad, th, td = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+    st = lib.hss_cache_check(limit, device, ctypes.byref(bad), ctypes.byref(th), ctypes.byref(td))
+    if st:
+        raise HssError(st, lib.hss_strerror(st).decode())
+    return {"mismatches": bad.value, "host_seconds": th.value, "device_seconds": td.value}
 
 
 class Search:

@@ -59,6 +59,10 @@ typedef struct {
                                  512: 1); 0 picks 4 / 2 / 1 */
     uint32_t use_graph;       /* 1: capture each batched launch sequence in a
                                  CUDA graph */
+    uint32_t host_build;      /* 1: build the factor cache with host threads
+                                 and upload it; 0 (default): build it with
+                                 kernels on the device (same arrays and values,
+                                 about 10x faster) */
 } hss_opts;
 
 /* Counters of one search call.  `pairs` and `candidates` are the reference's
@@ -108,9 +112,10 @@ const char* hss_strerror(int status);
 /* Last error message recorded on the handle (never NULL). */
 const char* hss_last_error(const hss_t* h);
 
-/* Builds the Gaussian factor cache for LIMIT on the host and makes it
- * resident on `device` (replaces Search::prepare and the uploads of
- * Search::run, gpu_search_v42.cu:354-432).  1 <= limit <= HSS_MAX_LIMIT. */
+/* Builds the Gaussian factor cache for LIMIT resident on `device`, by
+ * kernels on the device or (opts->host_build) on the host and uploaded
+ * (replaces Search::prepare and the uploads of Search::run,
+ * gpu_search_v42.cu:354-432).  1 <= limit <= HSS_MAX_LIMIT. */
 int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out);
 
 /* Releases the device cache and the handle (gpu_search_v42.cu:496-505). */
@@ -135,6 +140,17 @@ int hss_int32_peak(int device, double* ops_per_second, double* ms);
  * values) and its length stored in *count. */
 int hss_cache_inspect(uint64_t limit, uint64_t x, uint64_t* records, uint64_t* flattened,
                       uint64_t* cached, int64_t* re, int64_t* im, uint32_t cap, uint32_t* count);
+
+/* Builds the factor cache for LIMIT both ways - kernels on `device` (the
+ * default of hss_open) and host threads (hss_opts.host_build) - and compares
+ * every array entry by entry: smallest prime factors, segment offsets, hot
+ * and exact records, record owners, the prime-power index and both
+ * prime-power tables, and the reported sizes.  *mismatches receives the
+ * number of differing entries (0: identical); *host_seconds and
+ * *device_seconds (when not NULL) the two build times.  A verification entry
+ * point: no counterpart in the reference. */
+int hss_cache_check(uint64_t limit, int device, uint64_t* mismatches, double* host_seconds,
+                    double* device_seconds);
 
 /* Searches root rows first..last (1 <= first <= last <= limit) against all
  * m in [l, limit] with the given mode (one reference "batch" when last-first
