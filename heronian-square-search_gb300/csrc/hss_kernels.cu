@@ -903,6 +903,8 @@ struct BatchedShared {
 };
 
 constexpr uint32_t kRootsPerLane = 4;  // a warp claims 128 roots at a time
+constexpr uint32_t kChunk = 32 * kRootsPerLane;
+constexpr uint32_t kCarry = 32;        // pair-constant slots of events left over from earlier claims
 
 __device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t slot, uint32_t k, uint32_t flags) {
     return (uint64_t)j | ((uint64_t)slot << 32) | ((uint64_t)k << 40) | ((uint64_t)flags << 53);
@@ -913,7 +915,7 @@ __device__ __forceinline__ uint64_t batched_event_word(uint32_t j, uint32_t slot
 // records starting at s0[u].  Record r of the pass (lane-major order, so
 // consecutive records are consecutive in memory) is found by a binary search
 // over the lanes' inclusive prefix sums, then within the owner lane.
-template <bool DUAL>
+template <bool DUAL, bool FLUSH = false>
 __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t na,
                                              const PairCtx* wctx, const uint32_t (&cnt)[kRootsPerLane],
                                              const uint32_t (&s0)[kRootsPerLane], uint32_t lane,
@@ -930,11 +932,11 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         if (lane >= (uint32_t)d) incl += t;
     }
     const uint32_t total = __shfl_sync(kFull, incl, 31);
-    if (total == 0) return;
+    if (!FLUSH && total == 0) return;
     const uint32_t excl = incl - mine;
     auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
-        if (!index_ok(k, na, buf.error_flags) || !index_ok(slot, 32 * kRootsPerLane, buf.error_flags)) return 0u;
+        if (!index_ok(k, na, buf.error_flags) || !index_ok(slot, kChunk + kCarry, buf.error_flags)) return 0u;
         const uint2 r = cached_event((uint32_t)(ev >> 53), s_alpha[k], cache.hot[j], wctx[slot], a0 + k, j,
                                      (uint32_t)l, row, s_tab, kTabD2, (uint32_t)cache.limit, &buf, slots);
         acc.cand += r.x & 0xFFFFu;
@@ -945,6 +947,11 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
         push_hits(&buf, tags, a0 + k, j, (uint32_t)l, pair_m(wctx[slot]), row, false);
     };
+    if (FLUSH) {
+        // the item's last events (the row values are replaced next)
+        while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
+        return;
+    }
     for (uint32_t base = 0; base < total; base += 32) {
         const uint32_t r = base + lane;
         uint32_t owner = 0;
@@ -978,7 +985,26 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
             if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
-    while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
+}
+
+// Events still queued when a warp's claim ends keep their pair constants in
+// the warp's carry slots (kChunk + lane), so that they wait for the drains of
+// the next claim, whose constants replace slots 0 .. kChunk - 1.  Every read
+// precedes every write: a carried event may be carried again.
+__device__ __forceinline__ void carry_events(uint64_t* q, uint32_t qn, PairCtx* wctx, uint32_t lane) {
+    __syncwarp();
+    uint64_t ev = 0;
+    PairCtx c;
+    if (lane < qn) {
+        ev = q[lane];
+        c = wctx[(uint32_t)(ev >> 32) & 0xFFu];
+    }
+    __syncwarp();
+    if (lane < qn) {
+        wctx[kChunk + lane] = c;
+        q[lane] = (ev & ~(0xFFull << 32)) | ((uint64_t)(kChunk + lane) << 32);
+    }
+    __syncwarp();
 }
 
 template <int NT, int MINB>
@@ -986,18 +1012,17 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
                                                            uint32_t n_items, uint32_t alpha_cap,
                                                            const LaunchBuffers buf) {
     constexpr uint32_t kWarps = NT / 32;
-    constexpr uint32_t kChunk = 32 * kRootsPerLane;
     extern __shared__ __align__(16) unsigned char smem[];
     AlphaHot* s_alpha = reinterpret_cast<AlphaHot*>(smem);
     PairCtx* s_wctx = reinterpret_cast<PairCtx*>(s_alpha + alpha_cap);
-    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * kChunk);
+    uint64_t* s_queue = reinterpret_cast<uint64_t*>(s_wctx + kWarps * (kChunk + kCarry));
     RootReq* s_req = reinterpret_cast<RootReq*>(s_queue + kWarps * kQueue);
     uint8_t* s_tab = reinterpret_cast<uint8_t*>(s_req + kWarps * 32 * kReqPerLane);
     __shared__ BatchedShared S;
 
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid / 32;
     uint64_t* q = s_queue + warp * kQueue;
-    PairCtx* wctx = s_wctx + warp * kChunk;
+    PairCtx* wctx = s_wctx + warp * (kChunk + kCarry);
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     uint32_t qn = 0;
     for (uint32_t i = tid; i < kTable2Bytes; i += NT) s_tab[i] = buf.tables[kTableBytes + i];
@@ -1058,7 +1083,12 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
             if (__any_sync(kFull, any_dual))
                 batched_pass<true>(s_alpha, na, wctx, cnt_dual, s0, lane, cache, s_tab, a0, w.l, w.row, buf, q,
                                    qn, wreq, acc);
-            __syncwarp();
+            carry_events(q, qn, wctx, lane);
+        }
+        {
+            const uint32_t none[kRootsPerLane] = {};
+            batched_pass<false, true>(s_alpha, na, wctx, none, none, lane, cache, s_tab, a0, w.l, w.row, buf, q, qn,
+                                      wreq, acc);
         }
         flush_acc(acc, &buf.rows[w.row]);
     }
@@ -1757,7 +1787,7 @@ void build_residue_tables(uint8_t* out) {
 size_t batched_smem_bytes(int threads, uint32_t alpha_cap) {
     const uint32_t warps = (uint32_t)threads / 32;
     return (size_t)alpha_cap * sizeof(AlphaHot) +
-           (size_t)warps * 32 * kRootsPerLane * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
+           (size_t)warps * (kChunk + kCarry) * sizeof(PairCtx) + (size_t)warps * kQueue * sizeof(uint64_t) +
            (size_t)warps * 32 * kReqPerLane * sizeof(RootReq) + kTable2Bytes;
 }
 
