@@ -342,7 +342,17 @@ __device__ __forceinline__ uint32_t sub_mod(uint32_t a, uint32_t b, uint32_t m) 
 // kernels whose lanes meet both kinds and whose instruction cache is tight.
 // WIDE: `tab` is the wide copy (tables over two periods), so z residues are
 // indexed as S + d and S + M - d without a reduction; otherwise the compact one.
-template <int MODE, bool WIDE = false>
+// 32-bit multiply-add d = a b + c (mod 2^32), kept as one fused instruction so
+// that the residue coordinates go to the multiply-add pipe, not the integer ALU.
+__device__ __forceinline__ uint32_t imad(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
+// FUSED: coordinates by multiply-adds with the negated beta residues (worth it
+// where beta is fixed across the loop, so the negation is hoisted out of it).
+template <int MODE, bool WIDE = false, bool FUSED = false>
 __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float bi, uint32_t brw, uint32_t biw,
                                               bool cb, const PairCtx& c, const uint8_t* tab, Acc& acc,
                                               bool dual_rt = false) {
@@ -352,8 +362,32 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
     const uint32_t ar = a.ra & kMaskA, ai = a.ia & kMaskA, bra = brw & kMaskA, bia = biw & kMaskA;
     const uint32_t ad = (a.ra >> kShiftD) & kMaskD, adi = (a.ia >> kShiftD) & kMaskD;
     const uint32_t bd = (brw >> kShiftD) & kMaskD, bdi = (biw >> kShiftD) & kMaskD;
-    const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
-    const uint32_t q1 = ad * bd, q2 = adi * bdi, q3 = ad * bdi, q4 = adi * bd;
+    // coordinates of alpha beta (p = 0) and alpha conj(beta) (p = 1) in each
+    // field, all in [0, 2 M^2): X0 = ar br - ai bi + M^2, Y0 = ar bi + ai br,
+    // X1 = ar br + ai bi, Y1 = ai br - ar bi + M^2 (nbi = -bi mod 2^32)
+    uint32_t XA[2], YA[2], XDs[2], YDs[2];
+    if (FUSED) {
+        const uint32_t nbia = 0u - bia, nbdi = 0u - bdi;
+        XA[0] = imad(ar, bra, imad(ai, nbia, kSqA));
+        XA[1] = imad(ar, bra, ai * bia);
+        YA[0] = imad(ar, bia, ai * bra);
+        YA[1] = imad(ai, bra, imad(ar, nbia, kSqA));
+        XDs[0] = imad(ad, bd, imad(adi, nbdi, kSqD));
+        XDs[1] = imad(ad, bd, adi * bdi);
+        YDs[0] = imad(ad, bdi, adi * bd);
+        YDs[1] = imad(adi, bd, imad(ad, nbdi, kSqD));
+    } else {
+        const uint32_t p1 = ar * bra, p2 = ai * bia, p3 = ar * bia, p4 = ai * bra;
+        const uint32_t q1 = ad * bd, q2 = adi * bdi, q3 = ad * bdi, q4 = adi * bd;
+        XA[0] = p1 + kSqA - p2;
+        XA[1] = p1 + p2;
+        YA[0] = p3 + p4;
+        YA[1] = p4 + kSqA - p3;
+        XDs[0] = q1 + kSqD - q2;
+        XDs[1] = q1 + q2;
+        YDs[0] = q3 + q4;
+        YDs[1] = q4 + kSqD - q3;
+    }
     const float f1 = a.re * br, f2 = a.im * bi, f3 = a.re * bi, f4 = a.im * br;
     const uint32_t sA = c.sres & kMaskA, sD = (c.sres >> kShiftD) & kMaskD;
     const uint32_t sel = (c.sres >> 31) ? 4u : 2u;
@@ -361,10 +395,7 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
         const bool valid = p == 0 ? !(ca & cb) : !(ca | cb);
-        const uint32_t X = p ? p1 + p2 : p1 + kSqA - p2;
-        const uint32_t Y = p ? p4 + kSqA - p3 : p3 + p4;
-        const uint32_t XD = p ? q1 + q2 : q1 + kSqD - q2;
-        const uint32_t YD = p ? q4 + kSqD - q3 : q3 + q4;
+        const uint32_t X = XA[p], Y = YA[p], XD = XDs[p], YD = YDs[p];
         const float xf = p ? f1 + f2 : f1 - f2;
         const float yf = p ? f4 - f3 : f3 + f4;
         const bool gx = valid & area_gate(Y, c.dinv, c.dthr);  // (D, 4A) = (x, y)
@@ -981,7 +1012,7 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         for (uint32_t k = 0; k < na; ++k) {
             const AlphaHot a = s_alpha[k];
             uint32_t flags = 0;
-            if (live) flags = eval_fast<DUAL ? 1 : 0, true>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
+            if (live) flags = eval_fast<DUAL ? 1 : 0, true, true>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
             if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
         }
     }
