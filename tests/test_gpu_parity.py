@@ -49,6 +49,43 @@ def test_rows_match_oracle(searches, mode, limit, first, last):
     assert sorted(got.hits) == sorted(want["hits"])
 
 
+@pytest.mark.parametrize("limit", [1, 2, 3, 4, 5, 6, 10, 13, 25, 65])
+def test_smallest_limits(built, limit):
+    """Every row at the smallest limits (empty rows, a single pair, no split
+    prime at all), both paths."""
+    with Oracle(limit) as o:
+        want = o.search(1, limit)
+    with hss.Search(limit) as s:
+        for mode in ("batched", "plain"):
+            got = s.search(1, limit, mode=mode, rows=True)
+            for key in FIELDS:
+                assert got.counts[key] == want[key], (mode, key)
+            assert got.row_candidates == want["row_candidates"], mode
+
+
+def test_random_intervals(built):
+    """Seeded random limits and intervals (edges included: the last rows of a
+    limit, single rows), per row against the oracle, both paths."""
+    rng = random.Random(20261204)
+    cases = []
+    for _ in range(8):
+        limit = rng.randint(2000, 200000)
+        width = rng.choice([1, 2, 7, 16])
+        first = rng.choice([rng.randint(1, limit), limit - width + 1, 1])
+        first = max(1, min(first, limit - width + 1))
+        cases.append((limit, first, first + width - 1))
+    for limit, first, last in cases:
+        with Oracle(limit) as o:
+            want = o.search(first, last)
+        with hss.Search(limit) as s:
+            for mode in ("batched", "plain"):
+                got = s.search(first, last, mode=mode, rows=True)
+                for key in FIELDS:
+                    assert got.counts[key] == want[key], (limit, first, last, mode, key)
+                assert got.row_candidates == want["row_candidates"], (limit, first, last, mode)
+                assert sorted(got.hits) == sorted(want["hits"]), (limit, first, last, mode)
+
+
 @pytest.mark.parametrize("mode", ["batched", "plain"])
 def test_smoke_cases(searches, published, mode):
     for case in published["cases"]:
