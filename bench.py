@@ -352,8 +352,9 @@ def our_arm(args, rank, world, local_rank):
         t = json.loads(TRAFFIC.read_text())
         traffic = t.get("batched_kernel_bytes_per_launch")
         if traffic and PEAKS.exists():
-            groups = max(c["launches"] // 4, 1)  # one persistent launch per launch group
-            gbs = traffic * groups / (main_ms * 1e-3) / 1e9
+            # the measured case's DRAM bytes per logical pair, over this step's pairs
+            mc = t["measured_case"]
+            gbs = mc["bytes"] / mc["pairs"] * c["pairs"] / (main_ms * 1e-3) / 1e9
             peak_gbs = json.loads(PEAKS.read_text()).get("hbm_gbs")
             hbm = {"achieved_gbs": gbs, "peak_gbs": peak_gbs, "frac": gbs / peak_gbs if peak_gbs else None,
                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
