@@ -117,7 +117,7 @@ def test_full100k_interval(searches, published):
 
 
 @pytest.mark.parametrize("name", ["reference_interval", "v45_ab_interval", "cpu_v18_500000",
-                                  "cpu_v18_1160000"])
+                                  "cpu_v18_1160000", "high_interval_5862500"])
 def test_production_limit_pins(searches, published, name):
     case = next(c for c in published["cases"] if c["name"] == name)
     r = searches(case["limit"]).search(case["first"], case["last"])
