@@ -117,7 +117,8 @@ def test_full100k_interval(searches, published):
 
 
 @pytest.mark.parametrize("name", ["reference_interval", "v45_ab_interval", "cpu_v18_500000",
-                                  "cpu_v18_1160000", "high_interval_5862500"])
+                                  "cpu_v18_1160000", "high_interval_5862500", "heavy_row_1116389",
+                                  "heavy_row_1447225"])
 def test_production_limit_pins(searches, published, name):
     case = next(c for c in published["cases"] if c["name"] == name)
     r = searches(case["limit"]).search(case["first"], case["last"])
@@ -125,6 +126,18 @@ def test_production_limit_pins(searches, published, name):
         assert r.counts["pairs"] == case["pairs"]
     assert r.counts["candidates"] == case["candidates"]
     assert lines(r.hits) == case["results"]
+
+
+def test_heavy_batch_record(searches, published):
+    """The reference's heavy-root batch: the roots of branch weight >= 100 in
+    1116384..1120479 (166 of them), one interval each in one launch sequence,
+    as the heavy-root program searches them."""
+    case = next(c for c in published["cases"] if c["name"] == "heavy_batch_1116384")
+    roots = [l for l in range(case["first"], case["last"] + 1) if hss.branch_weight(l) >= case["min_weight"]]
+    assert len(roots) == case["rows"]
+    per, total = searches(case["limit"]).search_many([(l, l) for l in roots])
+    assert total.counts["candidates"] == case["candidates"]
+    assert total.hits == []
 
 
 def test_plain_equals_batched_at_production_limit(searches):
