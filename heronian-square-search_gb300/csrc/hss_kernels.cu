@@ -921,13 +921,14 @@ __device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, 
 
 // Persistent batched kernel.  CTAs pull items (row l, m-range); the row's
 // segment (scaled by 2) is staged in shared memory once per item.  Warps then
-// work on their own: each claims 32 roots m at a time, classifies them (one
-// per lane), keeps the pair constants in its shared slice, and walks the
+// work on their own: each claims 128 roots m at a time (4 per lane),
+// classifies them, keeps the pair constants in its shared slice, and walks the
 // valid m-side records in rounds of 32 - lane i of round r takes record
 // 32r + i of the concatenated segments, found with a shuffle search over the
 // lanes' prefix sums - running the row's values in lockstep.  Pairs of the
 // dual kind (both orientations live) go in a second pass of their own.
-// Events are drained from the warp queue before the warp's next 32 roots.
+// Events are drained 32 at a time; those left when a claim ends move to the
+// warp's carry slots, and the item's end drains the rest.
 struct BatchedShared {
     uint32_t item;
     uint32_t next_m;
