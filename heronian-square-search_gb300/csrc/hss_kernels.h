@@ -68,7 +68,7 @@ struct LaunchBuffers {
     unsigned int* next_item;    // work-queue cursor of the batched kernel
     unsigned int* error_flags;  // bit 0: shared-prime queue full; 1: pair lists over capacity; 2: exact queue full
     uint4* big_queue;           // shared-prime pairs too big for one warp's lists: kBigEntryWords
-                                // words each (the pair's descriptor, set up by the warp kernel)
+                                // words each (the pair's descriptor, written by the set-up kernel)
     unsigned int* big_count;
     unsigned int* big_next;     // cursor of the big-pair kernel over big_queue
     uint32_t big_cap;
