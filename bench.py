@@ -56,23 +56,32 @@ UNIT = "pairs/s"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC = ROOT / "profiles" / "traffic.json"
 
-# CPU sample of the batch: 64 jobs (rows spread over the batch, both
-# parities), each job one row over every STEP-th m; one job per host thread
-# at a time.
-SAMPLE_JOBS = 64
-SAMPLE_STEP = 4          # cpu_baseline of our arm (about 20 s on 16 Arm cores)
-REFERENCE_STEP = 8       # each step of the reference arm (about 10 s on 16 Arm cores)
+# CPU sample of the batch: every row of the batch, each over every STEP-th m
+# from a seeded offset in [0, STEP) (so m's residues are independent of l's);
+# one row per host thread at a time.  1/STEP of the batch's logical pairs.
+SAMPLE_SEED = 11
+SAMPLE_STEP = 64         # cpu_baseline of our arm and each step of the reference arm
+                         # (20 M logical pairs: about 8 s on 16 Arm cores)
 
 # serving stream
 SERVE_SEED = 5
 SERVE_REQUESTS = 12
-SERVE_RATE = 10.0        # requests per second (Poisson)
+SERVE_RATE = 10.0        # requests per second (Poisson) at LIMIT 10^7
 SERVE_MAX_LEN = 4096     # lengths log-uniform in [1, SERVE_MAX_LEN] roots
+SWEEP_LIMIT = 100_000    # rate sweep: requests of milliseconds, so the rates span under- to over-load
+SWEEP_RATES = (10.0, 30.0, 100.0, 300.0, 1000.0)
+SWEEP_WINDOW_S = 2.0     # requests per rate: rate x window, within [MIN, MAX]
+SWEEP_MIN_REQUESTS = 20
+SWEEP_MAX_REQUESTS = 200
 
-# batched uneven workload (--workload uneven)
+# batched uneven workload (config 4)
 UNEVEN_SEED = 4
-UNEVEN_INTERVALS = 64
+UNEVEN_INTERVALS = 256
 UNEVEN_PLAIN_CHECK = 4
+
+# config 2b: root edges 1..100,000
+C2B_LIMIT = 100_000
+C2B_CANDIDATES = 141_401_679_490
 
 
 def logical_pairs(first, last, limit=LIMIT):
@@ -132,28 +141,32 @@ class Clocks:
                 "power_w_max": max(r[2] for r in rows), "reasons": reasons, "samples": len(rows)}
 
 
-def sample_jobs(first=FIRST, rows=ROWS, jobs=SAMPLE_JOBS, step=SAMPLE_STEP):
-    """Job i: row first + 8i + (i mod 2) (spread over the batch, alternating
-    parity), m = l + (i mod step), then every step-th m."""
-    out = []
-    stride = max(rows // jobs, 1)
-    for i in range(jobs):
-        l = first + min(stride * i + (i % 2), rows - 1)
-        out.append((l, l + (i % step)))
-    return out
+def sample_jobs(first=FIRST, rows=ROWS, step=SAMPLE_STEP, seed=SAMPLE_SEED):
+    """Job i: row first + i, m = l + offset_i, l + offset_i + step, ... with
+    offset_i drawn from [0, step) by a seeded generator."""
+    rng = random.Random(seed)
+    return [(first + i, first + i + rng.randrange(step)) for i in range(rows)]
 
 
-def cpu_sample(step, jobs=SAMPLE_JOBS):
+def sample_description(step, pairs, threads, seconds=None):
+    took = f", {seconds:.1f} s" if seconds is not None else ""
+    return (f"every row of the batch over every {step}th m from a seeded offset ({pairs} logical pairs, "
+            f"1/{step} of the batch{took}), one row per host thread at a time, {threads} threads; "
+            "oracle restating src/search_v18.cpp")
+
+
+def cpu_sample(step, limit=LIMIT, first=FIRST, rows=ROWS):
     """The oracle (a restatement of the reference's CPU search) on a strided
     sample of the batch with all host threads; returns (pairs/s, seconds,
     threads, kind, pairs)."""
     from oracle import Oracle
     threads = os.cpu_count() or 1
-    with Oracle(LIMIT) as o:
+    jobs = sample_jobs(first, rows, step)
+    with Oracle(limit) as o:
         t = time.time()
-        r = o.sample(sample_jobs(jobs=jobs, step=step), step, threads=threads)
+        r = o.sample(jobs, step, threads=threads)
         sec = time.time() - t
-    return r["pairs"] / sec, sec, min(threads, jobs), "port", r["pairs"]
+    return r["pairs"] / sec, sec, min(threads, len(jobs)), "port", r["pairs"]
 
 
 def reference_arm(args, rank, world):
@@ -162,29 +175,29 @@ def reference_arm(args, rank, world):
     from oracle import Oracle, build as build_oracle
     build_oracle()
     threads = os.cpu_count() or 1
-    jobs = sample_jobs(step=REFERENCE_STEP)
+    step = args.cpu_sample
+    jobs = sample_jobs(step=step)
     vals, secs = [], []
     pairs = 0
     with Oracle(LIMIT) as o:
         for _ in range(args.warmup):
-            o.sample(jobs[:threads], REFERENCE_STEP * 64, threads=threads)
+            o.sample(jobs[:threads], step * 64, threads=threads)
         for _ in range(args.steps):
             t = time.time()
-            r = o.sample(jobs, REFERENCE_STEP, threads=threads)
+            r = o.sample(jobs, step, threads=threads)
             sec = time.time() - t
             pairs = r["pairs"]
             vals.append(pairs / sec)
             secs.append(sec)
     value = statistics.mean(vals)
-    sample = (f"{len(jobs)} jobs spread over the batch, each one row over every {REFERENCE_STEP}th m "
-              f"({pairs} logical pairs per step), {min(threads, len(jobs))} host threads")
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+    sample = sample_description(step, pairs, min(threads, len(jobs)))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic (the search interval itself; no dataset)",
             "config": {"workload": f"LIMIT={LIMIT}, root edges {FIRST}..{FIRST + ROWS - 1} (one reference batch); "
                                    "each step a strided sample of it on the host cores",
-                       "limit": LIMIT, "sample_step": REFERENCE_STEP, "sample_jobs": len(jobs)},
+                       "limit": LIMIT, "sample_step": step, "sample_jobs": len(jobs)},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": min(threads, len(jobs)), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -192,16 +205,40 @@ def reference_arm(args, rank, world):
     return 0
 
 
-def serving(s, seed=SERVE_SEED, n_req=SERVE_REQUESTS, rate=SERVE_RATE, max_len=SERVE_MAX_LEN):
-    """Seeded Poisson stream through the serving loop, then the same requests
-    one at a time (hss_search, batched path).  Latency = finish - submit."""
+def poisson_stream(seed, n_req, rate, max_len, limit):
+    """Seeded Poisson arrivals of interval requests: lengths log-uniform in
+    [1, max_len] roots, starts uniform in [1, limit - length + 1]."""
     rng = random.Random(seed)
     reqs, t = [], 0.0
     for _ in range(n_req):
         t += rng.expovariate(rate)
         length = min(max(int(round(math.exp(rng.uniform(0.0, math.log(max_len))))), 1), max_len)
-        first = rng.randint(1, LIMIT - length + 1)
+        first = rng.randint(1, limit - length + 1)
         reqs.append((t, first, first + length - 1))
+    return reqs
+
+
+def pct(v, q):
+    v = sorted(v)
+    return v[min(len(v) - 1, int(math.ceil(q * len(v))) - 1)]
+
+
+def replay_one_at_a_time(reqs, service_s):
+    """Latencies (ms) of the requests served one at a time in arrival order:
+    each starts when it has arrived and the previous one has finished, and
+    takes its measured service time."""
+    lat, clock = [], 0.0
+    for (at, _, _), svc in zip(reqs, service_s):
+        clock = max(clock, at) + svc
+        lat.append(1e3 * (clock - at))
+    return lat, clock
+
+
+def serve_stream(s, reqs, limit, alone=None, alone_modes=("plain",)):
+    """The stream through the serving loop (submissions at their arrival
+    times), then the same requests one at a time on each path in
+    `alone_modes` (service times measured, arrivals replayed).  Results must
+    be the same alone and in the mix."""
     s.serve_start()
     ids = []
     t0 = time.time()
@@ -213,32 +250,124 @@ def serving(s, seed=SERVE_SEED, n_req=SERVE_REQUESTS, rate=SERVE_RATE, max_len=S
     done = [s.wait(i) for i in ids]
     makespan = time.time() - t0
     s.serve_stop()
-    lat = sorted((d["finished_ns"] - d["submitted_ns"]) / 1e6 for d in done)
-    pairs = sum(logical_pairs(a, b) for _, a, b in reqs)
-    # one at a time, arrivals replayed: a request starts when it has arrived
-    # and the previous one has finished (service times measured)
-    seq_lat, clock, same = [], 0.0, True
-    for (at, a, b), d in zip(reqs, done):
-        t1 = time.time()
-        r = s.search(a, b)
-        svc = time.time() - t1
-        clock = max(clock, at) + svc
-        seq_lat.append(1e3 * (clock - at))
-        same &= all(r.counts[k] == d["counts"][k] for k in ("pairs", "candidates", "products", "processed"))
-        same &= sorted(r.hits) == sorted(d["hits"])
-    seq_lat.sort()
+    lat = [(d["finished_ns"] - d["submitted_ns"]) / 1e6 for d in done]
+    pairs = sum(logical_pairs(a, b, limit) for _, a, b in reqs)
+    out = {"requests": len(reqs), "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
+           "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99)}
+    same = True
+    for mode in alone_modes:
+        svc = []
+        for (_, a, b), d in zip(reqs, done):
+            t1 = time.time()
+            r = s.search(a, b, mode=mode)
+            svc.append(time.time() - t1)
+            same &= all(r.counts[k] == d["counts"][k] for k in ("pairs", "candidates", "products", "processed"))
+            same &= sorted(r.hits) == sorted(d["hits"])
+        seq, end = replay_one_at_a_time(reqs, svc)
+        out[f"one_at_a_time_{mode}"] = {"pairs_per_s": pairs / (end - reqs[0][0]), "p50_ms": pct(seq, 0.5),
+                                        "p99_ms": pct(seq, 0.99)}
+    out["results_same_alone_and_in_mix"] = bool(same)
+    return out
 
-    def pct(v, q):
-        return v[min(len(v) - 1, int(math.ceil(q * len(v))) - 1)]
 
-    return {"requests": n_req, "rate_per_s": rate, "lengths": f"log-uniform [1, {max_len}] roots", "seed": seed,
-            "pairs": pairs, "pairs_per_s": pairs / makespan, "makespan_s": makespan,
-            "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
-            "one_at_a_time": {"pairs_per_s": pairs / (clock - reqs[0][0]) if clock > reqs[0][0] else None,
-                              "p50_ms": pct(seq_lat, 0.5), "p99_ms": pct(seq_lat, 0.99)},
-            "results_same_alone_and_in_mix": bool(same),
-            "note": "offered load exceeds device capacity (mean request about 2.5e9 pairs); "
-                    "latency includes queueing; p99 of 12 requests is their maximum"}
+def serving(s, local_rank):
+    """Serving (continuous admission into double-buffered waves), against
+    the same requests one at a time: a rate sweep at LIMIT 10^5, where the
+    rates span under- to over-load, compared with the plain path (and the
+    batched path) one at a time; and one stream at LIMIT 10^7, where every
+    request is seconds of work, compared with the batched path one at a
+    time (the plain path would take minutes per request)."""
+    import hss
+    sweep = []
+    with hss.Search(SWEEP_LIMIT, device=local_rank) as small:
+        for rate in SWEEP_RATES:
+            n = max(SWEEP_MIN_REQUESTS, min(SWEEP_MAX_REQUESTS, int(rate * SWEEP_WINDOW_S)))
+            reqs = poisson_stream(SERVE_SEED + int(rate), n, rate, SERVE_MAX_LEN, SWEEP_LIMIT)
+            r = serve_stream(small, reqs, SWEEP_LIMIT, alone_modes=("plain", "batched"))
+            r["rate_per_s"] = rate
+            sweep.append(r)
+    reqs = poisson_stream(SERVE_SEED, SERVE_REQUESTS, SERVE_RATE, SERVE_MAX_LEN, LIMIT)
+    big = serve_stream(s, reqs, LIMIT, alone_modes=("batched",))
+    big["rate_per_s"] = SERVE_RATE
+    return {"lengths": f"log-uniform [1, {SERVE_MAX_LEN}] roots, uniform starts", "seed": SERVE_SEED,
+            "sweep": {"limit": SWEEP_LIMIT, "rates": sweep},
+            "production": dict(big, limit=LIMIT,
+                               note="offered load exceeds device capacity (mean request about 2.5e9 pairs); "
+                                    "latency includes queueing"),
+            "latency": "finish - submit (serving); replayed arrivals with measured service times (one at a time)"}
+
+
+def uneven(local_rank, count):
+    """Config-4 workload at LIMIT 10^7: a seeded prefix of `count` uneven
+    intervals in one hss_search_many call under a CUDA graph with the
+    autotuned kernel variant; every interval's counts checked against its own
+    hss_search, the smallest intervals also on the plain path."""
+    import hss
+    intervals = hss.uneven_intervals(UNEVEN_SEED, count, LIMIT)
+    pairs = sum(logical_pairs(a, b) for a, b in intervals)
+    with hss.Search(LIMIT, device=local_rank, use_graph=1) as s:
+        chosen, trials = s.autotune(FIRST, FIRST + 63)
+        s.search_many(intervals[:8])  # warm: graph instantiated, kernels loaded
+        t = time.time()
+        per, total = s.search_many(intervals)
+        wall = time.time() - t
+        c = total.counts
+        same = True
+        for (a, b), counts in zip(intervals, per):
+            r = s.search(a, b)
+            same &= all(r.counts[k] == counts[k] for k in ("pairs", "candidates", "products", "processed", "r16"))
+        small = sorted(range(len(intervals)), key=lambda i: logical_pairs(*intervals[i]))[:UNEVEN_PLAIN_CHECK]
+        plain_same, plain_ms, plain_pairs = True, 0.0, 0
+        for i in small:
+            r = s.search(*intervals[i], mode="plain")
+            plain_ms += r.counts["kernel_ms"]
+            plain_pairs += logical_pairs(*intervals[i])
+            plain_same &= all(r.counts[k] == per[i][k] for k in ("pairs", "candidates", "products", "processed"))
+    heavy = sum(1 for a, _ in intervals if hss.branch_weight(a) >= 100)
+    return {"intervals": len(intervals), "seed": UNEVEN_SEED, "limit": LIMIT, "pairs": pairs,
+            "rows": sum(b - a + 1 for a, b in intervals), "heavy_starts": heavy,
+            "value": pairs / (c["kernel_ms"] * 1e-3), "e2e_value": pairs / wall, "unit": UNIT,
+            "ms": c["kernel_ms"], "candidates": c["candidates"], "graph_launches": c["graph_launches"],
+            "gpu_launches": c["launches"], "autotuned": {k: chosen[k] for k in ("block_threads", "ctas_per_sm",
+                                                                                 "item_target")},
+            "every_interval_equals_its_own_search": bool(same),
+            "plain_smallest": {"intervals": len(small), "value": plain_pairs / (plain_ms * 1e-3) if plain_ms else None,
+                               "counts_equal": bool(plain_same)},
+            "heavy_rule": "10 % of starts moved to the next root of branch weight >= 100 "
+                          "(no root <= 1e7 has 6 distinct split primes)"}
+
+
+def config2b(local_rank):
+    """Root edges 1..100,000 at LIMIT 10^5 (5,000,050,000 logical pairs) on
+    the batched and the plain path; candidates and hits against the pinned
+    counts."""
+    import hss
+    with hss.Search(C2B_LIMIT, device=local_rank) as s:
+        s.search(1, 2000)  # warm
+        b = s.search(1, C2B_LIMIT)
+        p = s.search(1, C2B_LIMIT, mode="plain")
+    pairs = logical_pairs(1, C2B_LIMIT, C2B_LIMIT)
+    return {"limit": C2B_LIMIT, "first": 1, "last": C2B_LIMIT, "pairs": pairs,
+            "batched": {"value": pairs / (b.counts["kernel_ms"] * 1e-3), "ms": b.counts["kernel_ms"], "unit": UNIT},
+            "plain": {"value": pairs / (p.counts["kernel_ms"] * 1e-3), "ms": p.counts["kernel_ms"], "unit": UNIT},
+            "candidates": b.counts["candidates"], "candidates_pinned": C2B_CANDIDATES,
+            "counts_equal": b.counts["candidates"] == p.counts["candidates"] == C2B_CANDIDATES,
+            "hits": [list(h) for h in b.hits]}
+
+
+def cpu_configs():
+    """The CPU oracle on configs 1 and 2a end to end, all host threads."""
+    from oracle import Oracle
+    threads = os.cpu_count() or 1
+    out = {}
+    for name, limit, first, last in (("config1", 5000, 1, 5000), ("config2a", 70000, 11789, 11789)):
+        with Oracle(limit) as o:
+            t = time.time()
+            r = o.search(first, last, threads=threads)
+            sec = time.time() - t
+        out[name] = {"limit": limit, "first": first, "last": last, "seconds": sec, "pairs": r["pairs"],
+                     "value": r["pairs"] / sec, "candidates": r["candidates"], "threads": threads}
+    return out
 
 
 def uneven_arm(args, rank, world, local_rank):
@@ -331,7 +460,9 @@ def our_arm(args, rank, world, local_rank):
         s.close()
         return 0
     plain = s.search(first, last, mode="plain") if not args.no_plain else None
-    serve = serving(s) if not args.no_serving else None
+    serve = serving(s, local_rank) if not args.no_serving else None
+    unev = uneven(local_rank, args.intervals) if not args.no_uneven else None
+    c2b = config2b(local_rank) if not args.no_config2b else None
     # the same cache built by host threads and uploaded (the other way to open)
     t0 = time.time()
     with hss.Search(LIMIT, device=local_rank, host_build=1) as hb:
@@ -360,11 +491,10 @@ def our_arm(args, rank, world, local_rank):
                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
     cpu = None
     if not args.no_cpu:
-        cv, csec, ccores, kind, cpairs = cpu_sample(SAMPLE_STEP)
+        cv, csec, ccores, kind, cpairs = cpu_sample(args.cpu_sample)
         cpu = {"value": cv, "unit": UNIT, "cores": ccores, "kind": kind,
-               "sample": f"{SAMPLE_JOBS} jobs spread over the batch, each one row over every {SAMPLE_STEP}th m "
-                         f"({cpairs} logical pairs, {csec:.1f} s), one job per host thread at a time; "
-                         "oracle restating src/search_v18.cpp"}
+               "sample": sample_description(args.cpu_sample, cpairs, ccores, csec),
+               "configs": cpu_configs()}
     value = world * pairs / (dev_ms * 1e-3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -386,6 +516,8 @@ def our_arm(args, rank, world, local_rank):
             "batched_over_plain": plain.counts["kernel_ms"] / dev_ms,
             "counts_equal": all(plain.counts[k] == c[k] for k in ("pairs", "candidates", "products"))},
         "serving": serve,
+        "uneven": unev,
+        "config2b": c2b,
         "counts": {k: c[k] for k in ("pairs", "processed", "products", "candidates", "r16", "exact", "merged",
                                      "hits")},
         "roofline": {"bound": "int32", "achieved": achieved, "peak": peak_ops / 1e9, "unit": "Gop/s",
@@ -405,6 +537,43 @@ def our_arm(args, rank, world, local_rank):
     return 0
 
 
+def visible_gpus():
+    """GPUs this process can use (nvidia-smi's list, narrowed by
+    CUDA_VISIBLE_DEVICES); 0 where there is no driver."""
+    try:
+        out = subprocess.run(["nvidia-smi", "-L"], capture_output=True, text=True, timeout=60)
+    except (OSError, subprocess.TimeoutExpired):
+        return 0
+    n = sum(1 for line in out.stdout.splitlines() if line.startswith("GPU "))
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+    if visible is not None:
+        n = min(n, len([v for v in visible.split(",") if v.strip()]))
+    return n
+
+
+def spawn_ranks(args):
+    """--gpus N without a launcher: starts N local ranks of this script (one
+    per GPU, RANK / LOCAL_RANK / WORLD_SIZE / MASTER_* set, rendezvous on
+    127.0.0.1), as torch.distributed.run would; rank 0 prints the line.  Our
+    arm needs N visible GPUs and fails with a message otherwise; the
+    reference arm runs on the host cores and needs none."""
+    import socket
+    if args.impl != "reference":
+        have = visible_gpus()
+        if have < args.gpus:
+            print(f"bench.py: --gpus {args.gpus} needs {args.gpus} visible GPUs, found {have}", file=sys.stderr)
+            return 2
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    procs = []
+    for r in range(args.gpus):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(args.gpus),
+                   LOCAL_WORLD_SIZE=str(args.gpus), MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, str(Path(__file__).resolve())] + sys.argv[1:], env=env))
+    return max(p.wait() for p in procs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -414,13 +583,22 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-uneven", action="store_true")
+    ap.add_argument("--no-config2b", action="store_true")
     ap.add_argument("--workload", default="batch", choices=["batch", "uneven"])
     ap.add_argument("--intervals", type=int, default=UNEVEN_INTERVALS)
+    ap.add_argument("--cpu-sample", type=int, default=SAMPLE_STEP,
+                    help="stride of the CPU sample over m (1/K of the batch's pairs)")
     args = ap.parse_args()
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
     if "RANK" not in os.environ:
-        world = 1
+        if args.gpus > 1:
+            return spawn_ranks(args)
+        os.environ.update(RANK="0", LOCAL_RANK="0", WORLD_SIZE="1")
+    rank = int(os.environ["RANK"])
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}", file=sys.stderr)
+        return 2
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return reference_arm(args, rank, world)

@@ -9,7 +9,10 @@
 //   * stderr: "flattened N Gaussian values", "cached N Gaussian pair values",
 //     "prepared in S seconds" (sizes recomputed for the same limit);
 //   * the state file (when given) is read first: stored limit/end must match
-//     and resume >= FIRST_L, then the search resumes at `resume`;
+//     and FIRST_L <= resume <= LAST_L + 1, then the search resumes at
+//     `resume`; a file without a limit key (empty or truncated before it)
+//     starts the range afresh, as the reference does; a value that is not an
+//     integer is skipped (the reference's std::stoull would end the process);
 //   * results are appended as "l m n area", skipping triples already in the
 //     file; every hit has passed the device's 256-bit Heron recheck;
 //   * after every batch of at most 512 roots: state written to STATE.tmp then
@@ -136,7 +139,9 @@ int main(int argc, char** argv) {
             if (key == "resume") saved = v;
             if (key == "min_weight") stored_weight = v;
         }
-        if (stored_limit && (stored_limit != n || stored_end != last || saved < first ||
+        // a resume beyond last + 1 cannot come from this range (the
+        // reference would take it and search nothing); rejected here
+        if (stored_limit && (stored_limit != n || stored_end != last || saved < first || saved > last + 1 ||
                              (heavy_cli && stored_weight != min_weight))) {
             std::cerr << (heavy_cli ? "checkpoint does not match requested range or weight\n"
                                     : "checkpoint does not match requested range\n");

@@ -128,7 +128,6 @@ int ensure_rows(hss_t* h, size_t rows) {
     if (s) return s;
     h->rows_cap = cap;
     if (h->h_rows) cudaFreeHost(h->h_rows);
-    if (h->h_row_info) cudaFreeHost(h->h_row_info);
     h->h_rows = nullptr;
     HSS_CUDA(h, cudaMallocHost(&h->h_rows, cap * sizeof(RowCounts)));
     h->h_rows_cap = cap;
@@ -166,13 +165,15 @@ int grow_exact(hss_t* h) {
     return HSS_OK;
 }
 
-// Runs `call` again after enlarging the exact queue when it overflowed.
+// Runs `call` again after enlarging the exact queue when it overflowed (the
+// queue grows 4x per rerun, up to 2^28 items; h->call_reruns counts them).
 template <class Call>
 int with_exact_retry(hss_t* h, Call call) {
-    for (int attempt = 0;; ++attempt) {
+    for (uint32_t attempt = 0;; ++attempt) {
         h->exact_overflow = false;
+        h->call_reruns = attempt;
         const int s = call();
-        if (s == HSS_ERR_OVERFLOW && h->exact_overflow && attempt < 3 && grow_exact(h) == HSS_OK) continue;
+        if (s == HSS_ERR_OVERFLOW && h->exact_overflow && grow_exact(h) == HSS_OK) continue;
         return s;
     }
 }
@@ -193,6 +194,29 @@ int ensure_items(hss_t* h, size_t n) {
         HSS_CUDA(h, cudaMallocHost(&h->h_items, cap * sizeof(WorkItem)));
         h->h_items_cap = cap;
     }
+    return HSS_OK;
+}
+
+// The buffers of one launch sequence (hits, control words, the shared-prime,
+// big-pair, descriptor and exact-work queues, row counters), its stream and
+// call events.  A handle has one set; serving gives each of its lanes another
+// set over the same cache.
+int alloc_launch_buffers(hss_t* h) {
+    h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
+    h->merged_cap = (uint32_t)kMergedCap;
+    h->big_cap = 1u << 20;
+    h->desc_chunk = kDescChunk;
+    h->exact_cap = h->opts.exact_capacity ? std::min<uint32_t>(h->opts.exact_capacity, 1u << 28) : 1u << 24;
+    int s;
+    if ((s = device_alloc(h, &h->d_hits, h->hit_cap)) || (s = device_alloc(h, &h->d_ctrl, 8)) ||
+        (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
+        (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) ||
+        (s = device_alloc(h, &h->d_desc, (size_t)h->desc_chunk * kBigEntryWords)) ||
+        (s = device_alloc(h, &h->d_exact, h->exact_cap)) || (s = ensure_rows(h, 1024)))
+        return s;
+    if ((!h->stream && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) ||
+        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+        return fail(h, HSS_ERR_CUDA, "stream or event creation failed");
     return HSS_OK;
 }
 
@@ -724,23 +748,9 @@ int hss_open(uint64_t limit, int device, const hss_opts* opts, hss_t** out) {
     }
     std::vector<uint8_t> tables(kTableTotalBytes);
     build_residue_tables(tables.data());
-    h->hit_cap = h->opts.hit_capacity ? h->opts.hit_capacity : kDefaultHitCap;
-    h->merged_cap = (uint32_t)kMergedCap;
-    h->big_cap = 1u << 20;
-    h->desc_chunk = kDescChunk;
-    h->exact_cap = 1u << 24;
-    if ((s = upload(h, &h->d_tables, tables.data(), kTableTotalBytes)) || (s = device_alloc(h, &h->d_hits, h->hit_cap)) ||
-        (s = device_alloc(h, &h->d_ctrl, 8)) || (s = device_alloc(h, &h->d_merged, h->merged_cap)) ||
-        (s = device_alloc(h, &h->d_big, (size_t)h->big_cap * kBigEntryWords)) ||
-        (s = device_alloc(h, &h->d_desc, (size_t)h->desc_chunk * kBigEntryWords)) || (s = device_alloc(h, &h->d_exact, h->exact_cap)) ||
-        (s = ensure_rows(h, 1024))) {
+    if ((s = upload(h, &h->d_tables, tables.data(), kTableTotalBytes)) || (s = alloc_launch_buffers(h))) {
         hss_close(h);
         return s;
-    }
-    if ((!h->stream && cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) ||
-        cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
-        hss_close(h);
-        return HSS_ERR_CUDA;
     }
     *out = h;
     return HSS_OK;
@@ -757,6 +767,8 @@ void hss_close(hss_t* h) {
     if (h->h_items) cudaFreeHost(h->h_items);
     if (h->h_rows) cudaFreeHost(h->h_rows);
     if (h->h_row_info) cudaFreeHost(h->h_row_info);
+    if (h->h_ctrl) cudaFreeHost(h->h_ctrl);
+    if (h->h_slots) cudaFreeHost(h->h_slots);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
@@ -851,6 +863,7 @@ int search_locked(hss_t* h, uint64_t first, uint64_t last, int mode, hss_counts*
     out->merged_ms = merged_ms;
     out->launches = h->launches;
     out->graph_launches = h->call_graphs;
+    out->reruns = h->call_reruns;
     out->h2d_bytes = h->h2d_bytes;
     out->d2h_bytes = h->d2h_bytes;
     for (size_t r = 0; r < rows; ++r) {
@@ -951,6 +964,7 @@ int search_many_locked(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, 
     sum.merged_ms = merged_ms;
     sum.launches = h->launches;
     sum.graph_launches = h->call_graphs;
+    sum.reruns = h->call_reruns;
     sum.h2d_bytes = h->h2d_bytes;
     sum.d2h_bytes = h->d2h_bytes;
     size_t r = 0;
@@ -985,6 +999,17 @@ int search_many_locked(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, 
 }  // namespace
 
 // ------------------------------------------------------------------ serving
+//
+// Continuous admission.  Requests queue at hss_submit; a background loop
+// admits them while request slots and device state space are free, and runs
+// waves - a bounded slice of every admitted request - on two lanes (launch
+// buffers and a stream each, over the handle's cache), so one wave runs on
+// the device while the host harvests the previous one and forms the next.
+// Each admitted request owns a range of row records in a device arena sized
+// from free HBM at serve start: every wave ends with a kernel that writes its
+// row counters there, marked done, so a request's progress and counts stay
+// on the device until it completes and are read back once.  Admission waits
+// when the arena has no room for a request's rows.
 
 namespace hss {
 
@@ -992,103 +1017,244 @@ struct Request {
     uint64_t id = 0, first = 0, last = 0;
     uint64_t next_row = 0;  // next root to schedule
     uint64_t rows_done = 0;
+    uint64_t inflight = 0;  // rows in waves not yet settled
+    uint32_t slot = 0;      // first record of its rows in the device state arena
     uint64_t submitted_ns = 0, admitted_ns = 0, finished_ns = 0;
+    double ms_weighted = 0; // wave device time x its logical pairs in the wave
     hss_counts counts{};
     std::vector<DevHit> hits;
     int status = HSS_ERR_BUSY;
     bool admitted = false;
 };
 
-// One wave: a slice of every admitted request, run as one batched launch
-// sequence; row counters and hits are attributed back by row index.
+// A wave on a lane: its rows (index i of the wave) and their requests.
+struct Wave {
+    std::vector<RowRef> rows;
+    std::vector<Request*> owner;
+    bool live = false;
+};
+
+}  // namespace hss
+
+namespace {
+
+// A lane: a second set of launch buffers and a stream over h's cache (the
+// cache arrays and residue tables are shared, not owned).
+hss_t* make_lane(hss_t* h, int* status) {
+    hss_t* lane = new hss_t();
+    lane->device = h->device;
+    lane->limit = h->limit;
+    lane->opts = h->opts;
+    lane->opts.use_graph = 0;
+    lane->sm_count = h->sm_count;
+    lane->seg_off = h->seg_off;
+    lane->spf = h->spf;
+    lane->dev = h->dev;
+    lane->d_tables = h->d_tables;
+    int s = alloc_launch_buffers(lane);
+    if (!s && cudaMallocHost(&lane->h_ctrl, 8 * sizeof(unsigned int)) != cudaSuccess) s = HSS_ERR_MEMORY;
+    if (s) {
+        hss_close(lane);
+        *status = s;
+        return nullptr;
+    }
+    *status = HSS_OK;
+    return lane;
+}
+
+int ensure_slots(hss_t* lane, size_t n) {
+    if (n <= lane->slots_cap) return HSS_OK;
+    device_free(lane, lane->d_slots);
+    lane->d_slots = nullptr;
+    if (lane->h_slots) cudaFreeHost(lane->h_slots);
+    lane->h_slots = nullptr;
+    const size_t cap = std::max(n, (size_t)1024);
+    int s = device_alloc(lane, &lane->d_slots, cap);
+    if (s) return s;
+    HSS_CUDA(lane, cudaMallocHost(&lane->h_slots, cap * sizeof(uint32_t)));
+    lane->slots_cap = cap;
+    return HSS_OK;
+}
+
+// Enqueues a wave on its (idle) lane: row constants, the batched launch
+// groups, the scatter of its row counters into the requests' device state,
+// and the read-back of the control words.  Returns without waiting for the
+// device.
+int launch_wave(hss_t* h, hss_t* lane, const Wave& w) {
+    const size_t n = w.rows.size();
+    int s = begin_call(lane, n);
+    if (s) return s;
+    std::vector<uint64_t> ls(n);
+    for (size_t i = 0; i < n; ++i) ls[i] = w.rows[i].l;
+    if ((s = upload_row_info(lane, ls)) || (s = ensure_slots(lane, n))) return s;
+    for (size_t i = 0; i < n; ++i) lane->h_slots[i] = w.owner[i]->slot + (uint32_t)(w.rows[i].l - w.owner[i]->first);
+    HSS_CUDA(lane, cudaMemcpyAsync(lane->d_slots, lane->h_slots, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                   lane->stream));
+    if ((s = run_batched(lane, w.rows))) return s;
+    HSS_CUDA(lane, launch_scatter_rows(lane->d_rows, lane->d_slots, (uint32_t)n, h->d_state, lane->stream));
+    HSS_CUDA(lane, cudaEventRecord(lane->ev1, lane->stream));
+    HSS_CUDA(lane, cudaMemcpyAsync(lane->h_ctrl, lane->d_ctrl, 8 * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                                   lane->stream));
+    return HSS_OK;
+}
+
+// Waits for a lane's wave and collects its hits and device time; a wave whose
+// exact-work queue overflowed runs again (grown queue) before it counts.
+int finish_wave(hss_t* h, hss_t* lane, const Wave& w, std::vector<DevHit>* hits, double* ms) {
+    for (uint32_t attempt = 0;; ++attempt) {
+        HSS_CUDA(lane, cudaStreamSynchronize(lane->stream));
+        const unsigned int* ctrl = lane->h_ctrl;
+        if (ctrl[3] & 4u) {
+            lane->exact_overflow = true;
+            if (grow_exact(lane) != HSS_OK) return fail(lane, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+            if (int s = launch_wave(h, lane, w)) return s;
+            continue;
+        }
+        if (ctrl[3] & 1u) return fail(lane, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
+        if (ctrl[3] & 2u) return fail(lane, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
+        if (ctrl[3]) return fail(lane, HSS_ERR_OVERFLOW, "a device index check failed");
+        const uint32_t nh = std::min(ctrl[0], lane->hit_cap);
+        hits->resize(nh);
+        if (nh) HSS_CUDA(lane, cudaMemcpy(hits->data(), lane->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
+        float f = 0;
+        HSS_CUDA(lane, cudaEventElapsedTime(&f, lane->ev0, lane->ev1));
+        *ms = f;
+        return HSS_OK;
+    }
+}
+
+// Sums a completed request's row records from the device state arena into
+// its counters; every row must be marked done.
+int read_request_state(hss_t* h, Request* r) {
+    const size_t rows = (size_t)(r->last - r->first + 1);
+    std::vector<RowCounts> state(rows);
+    HSS_CUDA(h, cudaMemcpy(state.data(), h->d_state + r->slot, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < rows; ++i) {
+        if (state[i].pad != 1) return fail(h, HSS_ERR_STATE, "a request row was not recorded on the device");
+        add_row(&r->counts, state[i]);
+        r->counts.pairs += h->limit - (r->first + i) + 1;
+    }
+    r->counts.d2h_bytes += rows * sizeof(RowCounts);
+    return HSS_OK;
+}
+
+// Attributes a finished wave to its requests (under serve_mu) and completes
+// those whose rows are all done: counters from the device state, slot range
+// released.
+void settle_wave(hss_t* h, Wave& w, int status, const std::vector<DevHit>& hits, double ms,
+                 std::vector<Request*>& active) {
+    std::lock_guard<std::mutex> lock(h->serve_mu);
+    for (size_t i = 0; i < w.rows.size(); ++i) {
+        Request* r = w.owner[i];
+        --r->inflight;
+        if (status) {
+            r->status = status;
+            r->next_row = r->last + 1;  // schedule nothing more
+            continue;
+        }
+        r->ms_weighted += ms * (double)(h->limit - w.rows[i].l + 1);
+        ++r->rows_done;
+    }
+    for (const DevHit& hit : hits)
+        if (hit.row < w.owner.size()) w.owner[hit.row]->hits.push_back(hit);
+    const uint64_t t = now_ns();
+    for (size_t i = 0; i < active.size();) {
+        Request* r = active[i];
+        const uint64_t rows = r->last - r->first + 1;
+        const bool failed = r->status != HSS_ERR_BUSY;
+        // a request leaves when all its rows are done, or when it failed and
+        // no wave in flight still writes its state records
+        if (failed ? r->inflight > 0 : r->rows_done < rows) {
+            ++i;
+            continue;
+        }
+        if (!failed) {
+            const int s = read_request_state(h, r);
+            r->status = s ? s : HSS_OK;
+            r->counts.kernel_ms = r->ms_weighted / (double)std::max<uint64_t>(r->counts.pairs, 1);
+            r->counts.hits = r->hits.size();
+        }
+        r->finished_ns = t;
+        h->arena.release(r->slot, (uint32_t)rows);
+        active[i] = active.back();
+        active.pop_back();
+    }
+    w.rows.clear();
+    w.owner.clear();
+    w.live = false;
+    h->serve_cv.notify_all();
+}
+
 void serve_loop(hss_t* h) {
     cudaSetDevice(h->device);
     std::vector<Request*> active;
+    Wave waves[2];
+    int next_lane = 0;
     for (;;) {
-        std::vector<RowRef> rows;
-        std::vector<Request*> owner;
+        Wave w;
         {
             std::unique_lock<std::mutex> lock(h->serve_mu);
-            h->serve_cv.wait(lock, [&] { return h->serve_stop || !h->pending.empty() || !active.empty(); });
+            auto schedulable = [&] {
+                for (Request* r : active)
+                    if (r->next_row <= r->last) return true;
+                return false;
+            };
+            h->serve_cv.wait(lock, [&] {
+                return h->serve_stop || !h->pending.empty() || schedulable() || waves[0].live || waves[1].live;
+            });
             if (h->serve_stop) break;
-            // admission: request slots and free device memory (row counters,
-            // items and hits of its share of a wave)
+            // admission: a request slot and room for its rows in the device state arena
             while (!h->pending.empty() && active.size() < h->max_active) {
                 Request* r = h->requests[h->pending.front()];
-                size_t free_b = 0, total_b = 0;
-                cudaMemGetInfo(&free_b, &total_b);
-                size_t need = (size_t)(r->last - r->first + 1) * sizeof(RowCounts) + (64u << 20);
-                if (free_b < need && !active.empty()) break;
+                uint32_t slot = 0;
+                if (!h->arena.alloc((uint32_t)(r->last - r->first + 1), &slot)) break;
                 h->pending.pop_front();
+                r->slot = slot;
                 r->admitted = true;
                 r->admitted_ns = now_ns();
                 r->next_row = r->first;
                 active.push_back(r);
             }
+            // the wave: a share of the pair budget for every admitted request, oldest first
             const uint64_t budget = (uint64_t)h->wave_items << 20;
             const uint64_t share = std::max<uint64_t>(budget / std::max<size_t>(active.size(), 1), 1);
             for (Request* r : active) {
                 uint64_t taken = 0;
                 while (r->next_row <= r->last && (taken == 0 || taken + (h->limit - r->next_row + 1) <= share)) {
                     taken += h->limit - r->next_row + 1;
-                    rows.push_back(RowRef{r->next_row, (uint32_t)rows.size()});
-                    owner.push_back(r);
+                    w.rows.push_back(RowRef{r->next_row, (uint32_t)w.rows.size()});
+                    w.owner.push_back(r);
                     ++r->next_row;
+                    ++r->inflight;
                 }
             }
         }
-        std::vector<DevHit> found;
-        uint32_t nfound = 0;
-        double ms = 0;
-        int s;
-        {
-            std::lock_guard<std::mutex> g(h->gpu_mu);
-            s = with_exact_retry(h, [&] {
-                int r = begin_call(h, rows.size());
-                if (!r) {
-                    std::vector<uint64_t> ls(rows.size());
-                    for (size_t i = 0; i < rows.size(); ++i) ls[i] = rows[i].l;
-                    r = upload_row_info(h, ls);
-                }
-                if (!r) r = run_batched(h, rows);
-                if (!r) {
-                    found.clear();
-                    r = end_call(h, rows.size(), &ms, &found, &nfound);
-                }
-                return r;
-            });
-        }
-        std::lock_guard<std::mutex> lock(h->serve_mu);
-        for (size_t i = 0; i < rows.size(); ++i) {
-            Request* r = owner[i];
+        const bool launched = !w.rows.empty();
+        if (launched) {
+            hss_t* lane = h->lanes[next_lane];
+            waves[next_lane] = std::move(w);
+            waves[next_lane].live = true;
+            const int s = launch_wave(h, lane, waves[next_lane]);
             if (s) {
-                r->status = s;
-                continue;
+                cudaStreamSynchronize(lane->stream);
+                settle_wave(h, waves[next_lane], s, {}, 0, active);
             }
-            add_row(&r->counts, h->h_rows[i]);
-            r->counts.pairs += h->limit - rows[i].l + 1;
-            r->counts.kernel_ms += ms * (double)(h->limit - rows[i].l + 1);  // pair-weighted share, normalised below
-            ++r->rows_done;
+            next_lane ^= 1;
         }
-        for (const DevHit& hit : found)
-            if (hit.row < owner.size()) owner[hit.row]->hits.push_back(hit);
-        uint64_t t = now_ns();
-        for (size_t i = 0; i < active.size();) {
-            Request* r = active[i];
-            bool done = r->status != HSS_ERR_BUSY || r->rows_done == r->last - r->first + 1;
-            if (done) {
-                if (r->status == HSS_ERR_BUSY) r->status = HSS_OK;
-                r->finished_ns = t;
-                r->counts.kernel_ms /= (double)std::max<uint64_t>(r->counts.pairs, 1);
-                r->counts.hits = r->hits.size();
-                active[i] = active.back();
-                active.pop_back();
-            } else {
-                ++i;
-            }
+        // Lanes alternate, so waves[next_lane] is the older wave.  After a
+        // launch it is harvested (the new wave keeps the device busy
+        // meanwhile); with nothing new to launch, the oldest live wave is.
+        int i = next_lane;
+        if (!waves[i].live && !launched) i ^= 1;
+        if (waves[i].live) {
+            std::vector<DevHit> hits;
+            double ms = 0;
+            const int s = finish_wave(h, h->lanes[i], waves[i], &hits, &ms);
+            settle_wave(h, waves[i], s, hits, ms, active);
         }
-        h->serve_cv.notify_all();
     }
+    for (hss_t* lane : h->lanes)
+        if (lane) cudaStreamSynchronize(lane->stream);
 }
 
 int request_info(hss_t* h, Request* r, hss_request_info* info, hss_hit* hits, uint32_t cap) {
@@ -1115,6 +1281,29 @@ int hss_serve_start(hss_t* h, uint32_t max_active, uint32_t wave_mpairs) {
     if (!h) return HSS_ERR_ARGUMENT;
     std::lock_guard<std::mutex> lock(h->serve_mu);
     if (h->serving) return HSS_OK;
+    HSS_CUDA(h, cudaSetDevice(h->device));
+    // device state arena: opts.serve_state_kb, else 1/16 of free HBM up to 256 MiB
+    size_t free_b = 0, total_b = 0;
+    HSS_CUDA(h, cudaMemGetInfo(&free_b, &total_b));
+    size_t bytes = h->opts.serve_state_kb ? (size_t)h->opts.serve_state_kb << 10
+                                          : std::min<size_t>(free_b / 16, (size_t)256 << 20);
+    const uint32_t rows = (uint32_t)std::min<size_t>(bytes / sizeof(RowCounts), UINT32_MAX);
+    if (rows == 0) return fail(h, HSS_ERR_ARGUMENT, "serving state arena holds no row");
+    if (int s = device_alloc(h, &h->d_state, rows)) return s;
+    for (int i = 0; i < 2; ++i) {
+        int s = HSS_OK;
+        h->lanes[i] = make_lane(h, &s);
+        if (s) {
+            for (hss_t*& lane : h->lanes) {
+                if (lane) hss_close(lane);
+                lane = nullptr;
+            }
+            device_free(h, h->d_state);
+            h->d_state = nullptr;
+            return fail(h, s, "serving lane set-up failed");
+        }
+    }
+    h->arena.reset(rows);
     h->max_active = max_active ? max_active : 64;
     h->wave_items = wave_mpairs ? wave_mpairs : 256;
     h->serve_stop = false;
@@ -1128,6 +1317,8 @@ int hss_submit(hss_t* h, uint64_t first, uint64_t last, uint64_t* request_id) {
     if (first < 1 || first > last || last > h->limit) return fail(h, HSS_ERR_ARGUMENT, "need 1 <= first <= last <= limit");
     std::lock_guard<std::mutex> lock(h->serve_mu);
     if (!h->serving) return fail(h, HSS_ERR_ARGUMENT, "serving loop not started");
+    if (last - first + 1 > h->arena.size)
+        return fail(h, HSS_ERR_MEMORY, "request rows exceed the serving state arena");
     Request* r = new Request();
     r->id = h->next_id++;
     r->first = first;
@@ -1171,6 +1362,12 @@ int hss_serve_stop(hss_t* h) {
     for (auto& kv : h->requests) delete kv.second;
     h->requests.clear();
     h->pending.clear();
+    for (hss_t*& lane : h->lanes) {
+        if (lane) hss_close(lane);
+        lane = nullptr;
+    }
+    device_free(h, h->d_state);
+    h->d_state = nullptr;
     h->serving = false;
     return HSS_OK;
 }

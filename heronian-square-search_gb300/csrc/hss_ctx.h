@@ -16,7 +16,46 @@
 
 namespace hss {
 struct Request;
-}
+
+// First-fit allocator of row records in the serving state arena (host-side
+// bookkeeping of device memory allocated once at serve start).
+struct SlotArena {
+    uint32_t size = 0;
+    std::map<uint32_t, uint32_t> free;  // offset -> length of free runs
+
+    void reset(uint32_t n) {
+        size = n;
+        free.clear();
+        if (n) free[0] = n;
+    }
+    bool alloc(uint32_t n, uint32_t* off) {
+        for (auto it = free.begin(); it != free.end(); ++it) {
+            if (it->second < n) continue;
+            *off = it->first;
+            const uint32_t rest = it->second - n, at = it->first + n;
+            free.erase(it);
+            if (rest) free[at] = rest;
+            return true;
+        }
+        return false;
+    }
+    void release(uint32_t off, uint32_t n) {
+        auto next = free.lower_bound(off);
+        if (next != free.end() && off + n == next->first) {
+            n += next->second;
+            next = free.erase(next);
+        }
+        if (next != free.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == off) {
+                prev->second += n;
+                return;
+            }
+        }
+        free[off] = n;
+    }
+};
+}  // namespace hss
 
 struct hss_ctx {
     int device = 0;
@@ -49,6 +88,7 @@ struct hss_ctx {
     hss::ExactItem* d_exact = nullptr;    // exact work queue
     uint32_t exact_cap = 0;
     bool exact_overflow = false;          // the last launch group outgrew it
+    uint32_t call_reruns = 0;             // reruns of the current call after growing it
     uint4* d_merged = nullptr;
     uint32_t merged_cap = 0;
     uint8_t* d_tables = nullptr;
@@ -86,5 +126,15 @@ struct hss_ctx {
     uint64_t next_id = 1;
     std::map<uint64_t, hss::Request*> requests;
     std::deque<uint64_t> pending;
+    hss_ctx* lanes[2] = {nullptr, nullptr};  // launch lanes of the serving loop
+    hss::RowCounts* d_state = nullptr;        // per-request row records (device)
+    hss::SlotArena arena;                     // their allocation
+
+    // a lane's own buffers: control words read back (pinned) and the state
+    // record of each wave row (device, and its pinned staging)
+    unsigned int* h_ctrl = nullptr;
+    uint32_t* d_slots = nullptr;
+    uint32_t* h_slots = nullptr;
+    size_t slots_cap = 0;
 };
 

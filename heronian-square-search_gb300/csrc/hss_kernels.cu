@@ -874,7 +874,8 @@ __device__ __forceinline__ uint64_t make_event(uint32_t v, uint32_t k, uint32_t 
 
 // Appends the lanes' events to the warp's queue (ballot-aggregated); returns
 // true when the queue holds at least 32 events.  All 32 lanes must call it.
-__device__ __forceinline__ bool queue_push(uint64_t* q, uint32_t& count, bool has, uint64_t ev) {
+template <class Ev>
+__device__ __forceinline__ bool queue_push(Ev* q, uint32_t& count, bool has, Ev ev) {
     const uint32_t mask = __ballot_sync(kFull, has);
     if (!mask) return false;
     const uint32_t lane = threadIdx.x & 31;
@@ -889,12 +890,12 @@ __device__ __forceinline__ bool queue_push(uint64_t* q, uint32_t& count, bool ha
 // (bits 4-7); the warp then scans every request together, and hit(ev, tags)
 // queues the exact hit test of each possible orientation of the lane's event.
 // All 32 lanes must call it.
-template <class Handler, class HitFn>
-__device__ __forceinline__ void drain(uint64_t* q, uint32_t& count, uint32_t n, RootReq* wreq, unsigned int* err,
+template <class Ev, class Handler, class HitFn>
+__device__ __forceinline__ void drain(Ev* q, uint32_t& count, uint32_t n, RootReq* wreq, unsigned int* err,
                                       Handler handle, HitFn hit) {
     __syncwarp();
     const uint32_t lane = threadIdx.x & 31;
-    uint64_t ev = 0;
+    Ev ev = 0;
     uint32_t info = 0;
     if (lane < n) {
         ev = q[lane];
@@ -1699,6 +1700,17 @@ __global__ void __launch_bounds__(128) exact_kernel(const DeviceCache cache, con
     }
 }
 
+// Serving: a wave's row counters into the requests' device-resident state.
+__global__ void __launch_bounds__(128) scatter_rows_kernel(const RowCounts* __restrict__ rows,
+                                                           const uint32_t* __restrict__ slots, uint32_t n,
+                                                           RowCounts* __restrict__ state) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        RowCounts c = rows[i];
+        c.pad = 1;
+        state[slots[i]] = c;
+    }
+}
+
 // INT32 throughput probe: 8 independent chains per thread, each step one
 // IMAD and one shift/logic pair (the multiply and logic pipes the search loop
 // uses); the result is stored so nothing is eliminated.
@@ -1890,6 +1902,14 @@ cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const L
     if (e != cudaSuccess) return e;
     merged_big_kernel<<<ctas, kMergedThreads, big_smem, stream>>>(cache, buf);
     *launches += 1;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_rows(const RowCounts* rows, const uint32_t* slots, uint32_t n, RowCounts* state,
+                                cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = (n + 127) / 128 < 1024 ? (n + 127) / 128 : 1024;
+    scatter_rows_kernel<<<blocks, 128, 0, stream>>>(rows, slots, n, state);
     return cudaGetLastError();
 }
 

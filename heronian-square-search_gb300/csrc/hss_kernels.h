@@ -125,6 +125,12 @@ double int32_peak_ops(int device, int sm_count, double* ms);
 // Exact work queued by the search kernels; run after them.
 cudaError_t launch_exact(const DeviceCache& cache, const LaunchBuffers& buf, int ctas, cudaStream_t stream);
 
+// Serving: copies a wave's row counters rows[i] into the requests' device-
+// resident state, state[slots[i]], marked done (RowCounts::pad = 1), so a
+// request's per-row progress and counts stay on the device until it ends.
+cudaError_t launch_scatter_rows(const RowCounts* rows, const uint32_t* slots, uint32_t n, RowCounts* state,
+                                cudaStream_t stream);
+
 // Occupancy helper for the persistent grid.
 int batched_max_ctas_per_sm(int threads, int min_blocks, size_t smem);
 

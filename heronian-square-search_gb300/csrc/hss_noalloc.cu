@@ -10,7 +10,10 @@
 // exact kernel) with all per-call device scratch in one file-scope array of
 // kNoAllocBytes that is part of the library image, and host staging in static
 // buffers.  Every GPU that loads the library holds the array until the process
-// exits.
+// exits.  The array bounds the work of one launch, not the call: a call whose
+// rows have more shared-prime pairs than the array holds runs as several
+// launch groups, and a group whose exact-work queue fills runs again in
+// smaller pieces.
 //
 // Set-up: the array's name is a host-side stand-in, not a device address.
 // The first call on a device, with that device current, looks the address up
@@ -91,10 +94,11 @@ int scratch_on(hss_t* h, unsigned char** out) {
     return HSS_OK;
 }
 
-// Pairs of row l that can share a split prime with some m in [l, N].
-uint64_t shared_bound(const hss_t* h, uint64_t l) {
+// Pairs (l, m) with m in [m0, m1) that can share a split prime with l
+// (inclusion-exclusion over the distinct split primes of l).
+uint64_t shared_bound(const hss_t* h, uint64_t l, uint64_t m0, uint64_t m1) {
     NumberFactors f = factor_number(h->spf.data(), l);
-    uint64_t n = h->limit, total = 0;
+    uint64_t total = 0;
     for (uint32_t mask = 1; mask < (1u << f.count); ++mask) {
         uint64_t prod = 1;
         int bits = 0;
@@ -103,10 +107,10 @@ uint64_t shared_bound(const hss_t* h, uint64_t l) {
             if (mask & (1u << i)) {
                 prod *= f.primes[i];
                 ++bits;
-                if (prod > n) over = true;
+                if (prod > h->limit) over = true;
             }
         if (over) continue;
-        uint64_t cnt = n / prod - (l - 1) / prod;
+        const uint64_t cnt = (m1 - 1) / prod - (m0 - 1) / prod;
         total = (bits & 1) ? total + cnt : total - cnt;
     }
     return total;
@@ -118,34 +122,45 @@ uint64_t shared_bound(const hss_t* h, uint64_t l) {
         if (e_ != cudaSuccess) return fail(h, HSS_ERR_CUDA, cudaGetErrorString(e_)); \
     } while (0)
 
-int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits, uint32_t hit_cap,
-        uint32_t* nhits) {
-    const uint32_t rows = (uint32_t)(last - first + 1);
-    if (rows > kNaRows) return fail(h, HSS_ERR_LIMIT, "hss_search_noalloc: more than 64 root rows");
-    uint64_t shared = 0;
-    uint32_t alpha_cap = 1;
-    for (uint32_t r = 0; r < rows; ++r) {
-        shared += shared_bound(h, first + r);
-        alpha_cap = std::max(alpha_cap, h->seg_off[first + r + 1] - h->seg_off[first + r]);
-    }
-    if (shared > kNaMerged)
-        return fail(h, HSS_ERR_LIMIT, "hss_search_noalloc: more pairs sharing a split prime than the scratch holds");
-    NA_CUDA(cudaSetDevice(h->device));
-    unsigned char* base = nullptr;
-    if (int s = scratch_on(h, &base)) return s;
+// A piece of a call: row r of the call against m in [m0, m1).  A call is run
+// as launch groups of pieces that fit the scratch: their shared-prime pairs
+// within kNaMerged, their items within kNaItems.  A group whose exact-work or
+// big-pair queue overflows is run again as smaller groups (a lone piece is
+// halved by m-range), so the limits bound memory, not the interval.
+struct Piece {
+    uint32_t r, m0, m1;
+};
+constexpr uint32_t kNaPieces = 4096;  // pending pieces (a depth-first work stack)
+constexpr uint32_t kNaMinSpan = 64;   // a piece is not halved below this many roots
+Piece g_stack[kNaPieces];
+RowCounts g_host_sum[kNaRows];
 
-    // row constants and work items (each row cut into equal m-ranges)
-    const uint32_t per_row = kNaItems / rows;
+struct GroupResult {
+    float ms;
+    uint32_t launches;
+    uint64_t h2d, d2h;
+};
+
+// Runs pieces g_stack[lo, hi) as one launch group, adding its row counters to
+// g_host_sum and its hits to g_host_hits[*nh ...] (at most kNaHits kept,
+// *found counts them all).  Returns HSS_ERR_OVERFLOW, with nothing added, when
+// a queue of the scratch overflowed.
+int run_group(hss_t* h, unsigned char* base, uint32_t rows, uint32_t lo, uint32_t hi, uint32_t alpha_cap,
+              uint32_t* nh, uint64_t* found, GroupResult* res) {
+    const uint32_t npieces = hi - lo;
+    const uint32_t per_piece = kNaItems / npieces;
     uint32_t n_items = 0;
-    for (uint32_t r = 0; r < rows; ++r) {
-        const uint64_t l = first + r;
-        fill_row_info(h->spf.data(), h->seg_off.data(), h->limit, l, &g_host_rows[r]);
-        const uint64_t span = h->limit - l + 1;
-        const uint64_t pieces = std::min<uint64_t>(per_row, (span + 31) / 32);
-        const uint64_t tile = (span + pieces - 1) / pieces;
-        for (uint64_t m = l; m <= h->limit; m += tile)
+    uint64_t shared = 0;
+    for (uint32_t i = lo; i < hi; ++i) {
+        const Piece& pc = g_stack[i];
+        const uint64_t l = g_host_rows[pc.r].l;
+        shared += shared_bound(h, l, pc.m0, pc.m1);
+        const uint64_t span = pc.m1 - pc.m0;
+        const uint64_t parts = std::max<uint64_t>(1, std::min<uint64_t>(per_piece, (span + 31) / 32));
+        const uint64_t tile = (span + parts - 1) / parts;
+        for (uint64_t m = pc.m0; m < pc.m1; m += tile)
             g_host_items[n_items++] =
-                WorkItem{(uint32_t)l, (uint32_t)m, (uint32_t)std::min<uint64_t>(m + tile, h->limit + 1), r};
+                WorkItem{(uint32_t)l, (uint32_t)m, (uint32_t)std::min<uint64_t>(m + tile, pc.m1), pc.r};
     }
 
     LaunchBuffers b;
@@ -175,7 +190,6 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     cudaStream_t st = h->stream;
     NA_CUDA(cudaMemsetAsync(base + kOffCtrl, 0, kNaCtrl * sizeof(unsigned int), st));
     NA_CUDA(cudaMemsetAsync(base + kOffRows, 0, rows * sizeof(RowCounts), st));
-    NA_CUDA(cudaMemcpyAsync(base + kOffRowInfo, g_host_rows, rows * sizeof(RowInfo), cudaMemcpyHostToDevice, st));
     NA_CUDA(cudaMemcpyAsync(base + kOffItems, g_host_items, n_items * sizeof(WorkItem), cudaMemcpyHostToDevice, st));
     BatchedConfig cfg;
     cfg.threads = h->opts.block_threads ? (int)h->opts.block_threads : 256;
@@ -193,11 +207,107 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     NA_CUDA(cudaMemcpyAsync(g_host_ctrl, ctrl, sizeof g_host_ctrl, cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaMemcpyAsync(g_host_counts, b.rows, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaStreamSynchronize(st));
+    if (g_host_ctrl[3] & ~7u) return fail(h, HSS_ERR_CUDA, "hss_search_noalloc: a device index check failed");
     if (g_host_ctrl[3]) return fail(h, HSS_ERR_OVERFLOW, "hss_search_noalloc: a scratch queue overflowed");
-    const uint32_t nh = std::min(g_host_ctrl[0], kNaHits);
-    if (nh) NA_CUDA(cudaMemcpy(g_host_hits, b.hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
-    float ms = 0;
-    NA_CUDA(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    const uint32_t group_hits = std::min(g_host_ctrl[0], kNaHits);
+    const uint32_t room = kNaHits - *nh;
+    const uint32_t take = std::min(group_hits, room);
+    if (take) NA_CUDA(cudaMemcpy(g_host_hits + *nh, b.hits, take * sizeof(DevHit), cudaMemcpyDeviceToHost));
+    *nh += take;
+    *found += g_host_ctrl[0];
+    NA_CUDA(cudaEventElapsedTime(&res->ms, h->ev0, h->ev1));
+    for (uint32_t r = 0; r < rows; ++r) {
+        RowCounts& a = g_host_sum[r];
+        const RowCounts& c = g_host_counts[r];
+        a.candidates += c.candidates;
+        a.products += c.products;
+        a.processed += c.processed;
+        a.r16 += c.r16;
+        a.exact += c.exact;
+        a.merged += c.merged;
+        a.mproducts += c.mproducts;
+        a.mcandidates += c.mcandidates;
+        a.mr16 += c.mr16;
+    }
+    res->launches = 2 + merged_launches;
+    res->h2d = n_items * sizeof(WorkItem);
+    res->d2h = sizeof g_host_ctrl + rows * sizeof(RowCounts) + take * sizeof(DevHit);
+    return HSS_OK;
+}
+
+int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits, uint32_t hit_cap,
+        uint32_t* nhits) {
+    const uint32_t rows = (uint32_t)(last - first + 1);
+    if (rows > kNaRows) return fail(h, HSS_ERR_LIMIT, "hss_search_noalloc: more than 64 root rows");
+    uint32_t alpha_cap = 1;
+    for (uint32_t r = 0; r < rows; ++r)
+        alpha_cap = std::max(alpha_cap, h->seg_off[first + r + 1] - h->seg_off[first + r]);
+    NA_CUDA(cudaSetDevice(h->device));
+    unsigned char* base = nullptr;
+    if (int s = scratch_on(h, &base)) return s;
+
+    // row constants of the whole call, uploaded once
+    for (uint32_t r = 0; r < rows; ++r)
+        fill_row_info(h->spf.data(), h->seg_off.data(), h->limit, first + r, &g_host_rows[r]);
+    NA_CUDA(cudaMemcpyAsync(base + kOffRowInfo, g_host_rows, rows * sizeof(RowInfo), cudaMemcpyHostToDevice,
+                            h->stream));
+    memset(g_host_sum, 0, sizeof g_host_sum);
+
+    // work stack: whole rows, last row at the bottom
+    uint32_t top = 0;
+    for (uint32_t r = rows; r-- > 0;)
+        g_stack[top++] = Piece{r, (uint32_t)(first + r), (uint32_t)(h->limit + 1)};
+    uint32_t max_group = kNaRows, nh = 0, groups = 0;
+    uint64_t found = 0, h2d = rows * sizeof(RowInfo), d2h = 0;
+    double ms = 0;
+    uint32_t launches = 0;
+    while (top) {
+        // a piece whose shared-prime pairs alone exceed the queue is halved
+        const Piece& t = g_stack[top - 1];
+        if (shared_bound(h, g_host_rows[t.r].l, t.m0, t.m1) > kNaMerged) {
+            if (top + 1 > kNaPieces || t.m1 - t.m0 < 2 * kNaMinSpan)
+                return fail(h, HSS_ERR_OVERFLOW, "hss_search_noalloc: work stack full");
+            const Piece p = t;
+            const uint32_t mid = p.m0 + (p.m1 - p.m0) / 2;
+            g_stack[top - 1] = Piece{p.r, mid, p.m1};
+            g_stack[top++] = Piece{p.r, p.m0, mid};
+            continue;
+        }
+        // the group: pieces from the top while their shared-prime pairs fit
+        uint32_t lo = top;
+        uint64_t bound = 0;
+        while (lo > 0 && top - lo < max_group) {
+            const Piece& q = g_stack[lo - 1];
+            const uint64_t b = shared_bound(h, g_host_rows[q.r].l, q.m0, q.m1);
+            if (b > kNaMerged || bound + b > kNaMerged) break;
+            bound += b;
+            --lo;
+        }
+        GroupResult res{};
+        const int s = run_group(h, base, rows, lo, top, alpha_cap, &nh, &found, &res);
+        if (s == HSS_ERR_OVERFLOW) {
+            // run again smaller: half the pieces, or a lone piece halved
+            if (top - lo > 1) {
+                max_group = (top - lo) / 2;
+                continue;
+            }
+            const Piece p = g_stack[lo];
+            if (top + 1 > kNaPieces || p.m1 - p.m0 < 2 * kNaMinSpan)
+                return fail(h, HSS_ERR_OVERFLOW, "hss_search_noalloc: a scratch queue overflowed");
+            const uint32_t mid = p.m0 + (p.m1 - p.m0) / 2;
+            g_stack[lo] = Piece{p.r, mid, p.m1};
+            g_stack[top++] = Piece{p.r, p.m0, mid};
+            continue;
+        }
+        if (s) return s;
+        top = lo;
+        ++groups;
+        ms += res.ms;
+        launches += res.launches;
+        h2d += res.h2d;
+        d2h += res.d2h;
+        max_group = std::min<uint32_t>(kNaRows, max_group * 2);
+    }
 
     std::sort(g_host_hits, g_host_hits + nh, [](const DevHit& x, const DevHit& y) {
         if (x.l != y.l) return x.l < y.l;
@@ -211,7 +321,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
                                        g_host_hits);
     memset(out, 0, sizeof *out);
     for (uint32_t r = 0; r < rows; ++r) {
-        const RowCounts& c = g_host_counts[r];
+        const RowCounts& c = g_host_sum[r];
         out->pairs += h->limit - (first + r) + 1;
         out->processed += c.processed;
         out->products += c.products;
@@ -223,12 +333,14 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
         out->merged_candidates += c.mcandidates;
         out->merged_r16 += c.mr16;
     }
-    const uint32_t found = g_host_ctrl[0] > kNaHits ? g_host_ctrl[0] : unique;
-    out->hits = found;
+    const uint64_t all = found > kNaHits ? found : unique;
+    out->hits = all;
     out->kernel_ms = ms;
-    out->launches = 2 + merged_launches;
-    out->h2d_bytes = rows * sizeof(RowInfo) + n_items * sizeof(WorkItem);
-    out->d2h_bytes = sizeof g_host_ctrl + rows * sizeof(RowCounts) + nh * sizeof(DevHit);
+    out->launches = launches;
+    out->graph_launches = 0;
+    out->h2d_bytes = h2d;
+    out->d2h_bytes = d2h;
+    (void)groups;
     for (uint32_t i = 0; i < unique && i < hit_cap && hits; ++i) {
         hits[i].l = g_host_hits[i].l;
         hits[i].m = g_host_hits[i].m;
@@ -238,7 +350,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
         hits[i].heron_ok = g_host_hits[i].heron_ok;
         hits[i].reserved = 0;
     }
-    if (nhits) *nhits = found;
+    if (nhits) *nhits = (uint32_t)std::min<uint64_t>(all, UINT32_MAX);
     return HSS_OK;
 }
 

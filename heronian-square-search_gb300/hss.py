@@ -28,7 +28,8 @@ class HssOpts(ctypes.Structure):
     _fields_ = [("prep_threads", ctypes.c_uint32), ("hit_capacity", ctypes.c_uint32),
                 ("block_threads", ctypes.c_uint32), ("item_target", ctypes.c_uint32),
                 ("ctas_per_sm", ctypes.c_uint32), ("use_graph", ctypes.c_uint32),
-                ("host_build", ctypes.c_uint32)]
+                ("host_build", ctypes.c_uint32), ("exact_capacity", ctypes.c_uint32),
+                ("serve_state_kb", ctypes.c_uint32)]
 
 
 class HssCounts(ctypes.Structure):
@@ -40,7 +41,8 @@ class HssCounts(ctypes.Structure):
                 ("merged_products", ctypes.c_uint64), ("merged_candidates", ctypes.c_uint64),
                 ("merged_r16", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64),
                 ("d2h_bytes", ctypes.c_uint64), ("launches", ctypes.c_uint32),
-                ("graph_launches", ctypes.c_uint32)]
+                ("graph_launches", ctypes.c_uint32), ("reruns", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
     def as_dict(self) -> Dict[str, float]:
         return {name: getattr(self, name) for name, _ in self._fields_}

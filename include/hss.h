@@ -63,6 +63,13 @@ typedef struct {
                                  and upload it; 0 (default): build it with
                                  kernels on the device (same arrays and values,
                                  about 10x faster) */
+    uint32_t exact_capacity;  /* initial exact-work queue items (0: 1<<24); a
+                                 launch group that outgrows the queue makes the
+                                 call grow it 4x (up to 1<<28) and run again */
+    uint32_t serve_state_kb;  /* serving: device memory for the admitted
+                                 requests' row records, 80 bytes per root row
+                                 (0: 1/16 of free HBM at serve start, at most
+                                 256 MiB); admission waits for room in it */
 } hss_opts;
 
 /* Counters of one search call.  `pairs` and `candidates` are the reference's
@@ -90,6 +97,9 @@ typedef struct {
     uint64_t d2h_bytes;          /* device-to-host bytes copied by the call */
     uint32_t launches;           /* kernels launched by the call */
     uint32_t graph_launches;     /* CUDA graph launches of the call (opts.use_graph) */
+    uint32_t reruns;             /* times the call ran again after growing the
+                                    exact-work queue */
+    uint32_t reserved;
 } hss_counts;
 
 /* A hit (l <= m <= n, gcd 1), with the signed 4A of the representation that
@@ -183,9 +193,14 @@ int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tu
  * nothing: its device scratch is one array of about 23 MiB that is static in
  * the library (every GPU that loads the library holds it until the process
  * exits), its host staging is static too, and the handle's cache, stream and
- * tables (made by hss_open) are the inputs.  Limits per call: at most 64 root
- * rows and at most 2^20 pairs sharing a split prime (HSS_ERR_LIMIT beyond
- * them); up to 4096 hits kept.  The first call on a device looks up the
+ * tables (made by hss_open) are the inputs.  Limit per call: at most 64 root
+ * rows (HSS_ERR_LIMIT beyond that); up to 4096 hits kept.  The array holds
+ * 2^20 pairs sharing a split prime, 2^16 exact-work items and 2^13 big
+ * shared-prime pairs at a time, so a call runs as several launch groups
+ * when its rows need more (a row at LIMIT 10^7 has about 85,000 such pairs:
+ * about 12 rows per group), and a group whose exact-work or big-pair queue
+ * fills is run again in smaller pieces (down to 64 roots of one row, then
+ * HSS_ERR_OVERFLOW).  The first call on a device looks up the
  * array's device address (cudaGetSymbolAddress) and should come before any
  * stream capture.  Calls share the array: they are serialised within the
  * process, clear what must start at zero, and calls that overlap on the GPU

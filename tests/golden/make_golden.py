@@ -2,7 +2,9 @@
 """Generate golden vectors by running the reference's own CPU search.
 
 The reference binary is compiled unchanged from its single source file
-(src/search_v18.cpp) by ``make -C oracle ref`` into ``oracle/_ref/search``.
+(src/search_v18.cpp) by ``make -C oracle ref REFERENCE=<checkout>`` into
+``oracle/_ref/search`` (the checkout: $HSS_REFERENCE, else ``reference``
+beside this repository).
 This script runs it through its own command line
 (``search LIMIT FIRST LAST THREADS STATE RESULTS``, src/search_v18.cpp:532-572)
 on each case below, in a scratch directory, with the coverage file pointed at
@@ -16,6 +18,12 @@ with inert primes, even rows, prime powers of 5 and 13, rows with four split
 primes, and rows at the production limit 10^7.
 
 Run here, where the reference checkout exists:  python tests/golden/make_golden.py
+
+``--rows LIMIT FIRST LAST`` instead runs every root row of the interval as its
+own single-threaded run of the reference binary (as many at once as there
+are cores) and stores the per-row candidate counts in
+``reference_rows_<LIMIT>_<FIRST>_<LAST>.json``: the reference itself reports
+only interval totals, so per-row pins need one run per row.
 """
 import json
 import os
@@ -65,8 +73,41 @@ def run_case(limit, first, last, threads, work):
             "wall_seconds": round(time.time() - start, 1)}
 
 
+def ensure_binary():
+    sys.path.insert(0, str(REPO))
+    from __graft_entry__ import reference_checkout
+    reference = reference_checkout()
+    if reference is None:
+        raise SystemExit("no reference checkout: set HSS_REFERENCE")
+    subprocess.run(["make", "-C", str(REPO / "oracle"), "ref", f"REFERENCE={reference}"], check=True)
+
+
+def per_row(limit, first, last):
+    from concurrent.futures import ThreadPoolExecutor
+    ensure_binary()
+    out = HERE / f"reference_rows_{limit}_{first}_{last}.json"
+    start = time.time()
+    with tempfile.TemporaryDirectory() as tmp, ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as pool:
+        runs = list(pool.map(lambda l: run_case(limit, l, l, 1, Path(tmp)), range(first, last + 1)))
+    out.write_text(json.dumps({
+        "generator": f"tests/golden/make_golden.py --rows {limit} {first} {last}",
+        "reference_binary": "src/search_v18.cpp built by `make -C oracle ref`",
+        "limit": limit, "first": first, "last": last,
+        "pairs": [r["pairs"] for r in runs], "candidates": [r["candidates"] for r in runs],
+        "results": [line for r in runs for line in r["results"]],
+        "wall_seconds": round(time.time() - start, 1)}) + "\n")
+    return 0
+
+
 def main():
-    subprocess.run(["make", "-C", str(REPO / "oracle"), "ref"], check=True)
+    if len(sys.argv) == 5 and sys.argv[1] == "--rows":
+        return per_row(*(int(x) for x in sys.argv[2:]))
+    sys.path.insert(0, str(REPO))
+    from __graft_entry__ import reference_checkout
+    reference = reference_checkout()
+    if reference is None:
+        raise SystemExit("no reference checkout: set HSS_REFERENCE")
+    subprocess.run(["make", "-C", str(REPO / "oracle"), "ref", f"REFERENCE={reference}"], check=True)
     out = HERE / "reference_runs.json"
     runs = json.loads(out.read_text())["runs"] if out.exists() else []
     have = {(r["limit"], r["first"], r["last"]) for r in runs}

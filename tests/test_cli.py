@@ -116,3 +116,71 @@ def test_existing_results_are_not_duplicated(built, tmp_path):
     r = run([70000, 11789, 11789, results], tmp_path)
     assert r.returncode == 0
     assert results.read_text() == "11789 68104 68595 284239560530875680\n"
+
+
+def test_corrupt_checkpoints_rejected_before_device(built, tmp_path):
+    """Host-side fault injection on the state file, decided before any device
+    work: a file truncated after its limit (end missing), or one whose
+    resume lies beyond the range, exits 2 and is left untouched."""
+    state = tmp_path / "s.txt"
+    for text in ("version 1\nlimit 5000\nbeg", "version 1\nlimit 5000\nbegin 1\nend 5000\nresume 6000\ncandidates 1\n",
+                 "version 1\nlimit 5000\nbegin 1\nend 50"):
+        state.write_text(text)
+        r = run([5000, 1, 5000, "r.txt", 0, state], tmp_path)
+        assert r.returncode == 2, text
+        assert "checkpoint does not match requested range" in r.stderr
+        assert state.read_text() == text
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("text", ["", "version 1\nlim", "garbage here\nlimit five\nresume x\n"])
+def test_unreadable_checkpoint_restarts_the_range(built, tmp_path, text):
+    """A state file with no readable limit (empty, truncated before it, or
+    not numbers) starts the range afresh, as the reference's parser does; a
+    stale STATE.tmp left by a killed run is overwritten.  The result equals
+    a run without a state file."""
+    limit, first, last = 3000, 1, 700
+    clean = tmp_path / "clean-state.txt"
+    assert run([limit, first, last, tmp_path / "r0.txt", 0, clean], tmp_path).returncode == 0
+    state = tmp_path / "s.txt"
+    state.write_text(text)
+    (tmp_path / "s.txt.tmp").write_text("half-written\n")
+    r = run([limit, first, last, tmp_path / "r1.txt", 0, state], tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert read_state(state) == read_state(clean)
+    assert progress_chain_ok(r.stdout, first, last)
+    assert not (tmp_path / "s.txt.tmp").exists()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("sig", ["SIGTERM", "SIGINT"])
+def test_signal_stops_at_a_batch_boundary(built, tmp_path, sig):
+    """SIGTERM / SIGINT sent to a running search (as gpu_queue.request_stop
+    does, scripts/gpu_queue.py:280-286) after its first PROGRESS line: the
+    process finishes the batch in flight, writes a checkpoint on a 512-root
+    boundary and exits 0 (gpu_search_v42.cu:93-101, 456); resuming from it
+    completes the range, and the two runs' candidates add up to an
+    uninterrupted run's."""
+    import signal
+    import hss
+    limit, first, last = 10_000_000, 7_500_000, 7_502_559  # five batches of 512 roots
+    state, results = tmp_path / "s.txt", tmp_path / "r.txt"
+    p = subprocess.Popen([str(BINARY), str(limit), str(first), str(last), str(results), "0", str(state)],
+                         cwd=tmp_path, text=True, stdout=subprocess.PIPE, stderr=subprocess.PIPE)
+    lines = [p.stdout.readline()]
+    assert lines[0].startswith("PROGRESS resume "), lines
+    p.send_signal(getattr(signal, sig))
+    out, err = p.communicate(timeout=600)
+    lines += out.splitlines()
+    assert p.returncode == 0, err
+    v = read_state(state)
+    assert (v["resume"] - first) % 512 == 0 and first + 512 <= v["resume"] <= last
+    assert progress_chain_ok("\n".join(lines), first, v["resume"] - 1)
+    c1 = v["candidates"]
+    r2 = run([limit, first, last, results, 0, state], tmp_path)
+    assert r2.returncode == 0, r2.stderr
+    v2 = read_state(state)
+    assert v2["begin"] == v["resume"] and v2["resume"] == last + 1
+    assert progress_chain_ok(r2.stdout, v["resume"], last)
+    with hss.Search(limit) as s:
+        assert c1 + v2["candidates"] == s.search(first, last).counts["candidates"]

@@ -201,3 +201,65 @@ def test_maximum_limit_rows(built):
                     assert got.counts[key] == want[key], (first, mode, key)
                 assert got.row_candidates == want["row_candidates"]
                 assert sorted(got.hits) == sorted(want["hits"])
+
+
+def test_exact_queue_growth_keeps_counts(searches):
+    """A handle opened with a small exact-work queue (1024 items): the launch
+    group outgrows it (8 rows at LIMIT 10^7 queue thousands), the call grows
+    the queue 4x and runs again until it fits, and the counts equal a default
+    handle's."""
+    first, last = 7_500_000, 7_500_007
+    want = searches(10 ** 7).search(first, last)
+    assert want.counts["exact"] > 1024
+    with hss.Search(10 ** 7, exact_capacity=1024) as s:
+        got = s.search(first, last)
+        assert got.counts["reruns"] >= 1
+        for key in FIELDS + ("exact",):
+            assert got.counts[key] == want.counts[key], key
+        assert got.hits == want.hits
+        again = s.search(first, last)  # the grown queue stays with the handle
+        assert again.counts["reruns"] == 0
+        assert again.counts["candidates"] == want.counts["candidates"]
+
+
+def test_serving_admission_waits_for_device_state(built):
+    """Admission binds on device memory: with a serving state arena of
+    160 KiB (2048 row records of 80 bytes), a request whose rows do not fit
+    beside those admitted waits until they finish; one larger than the
+    whole arena is refused at submit.  Every result equals the request run
+    alone."""
+    reqs = [(1, 1500), (20000, 21400), (50000, 51000), (99000, 99999), (11789, 11789)]
+    with hss.Search(100000, serve_state_kb=160) as s:
+        alone = [s.search(a, b) for a, b in reqs]
+        s.serve_start(max_active=8, wave_mpairs=4)
+        try:
+            with pytest.raises(hss.HssError):
+                s.submit(1, 3000)
+            ids = [s.submit(a, b) for a, b in reqs]
+            done = [s.wait(i) for i in ids]
+        finally:
+            s.serve_stop()
+    assert done[1]["admitted_ns"] >= done[0]["finished_ns"]  # 1500 + 1401 rows > 2048
+    for want, got in zip(alone, done):
+        assert got["status"] == 0
+        for key in FIELDS:
+            assert got["counts"][key] == want.counts[key], key
+        assert sorted(got["hits"]) == sorted(want.hits)
+
+
+def test_production_batch_rows_match_reference_binary(searches):
+    """Every one of the 512 rows of the production batch at LIMIT 10^7,
+    on both paths, against the reference binary run on each row alone
+    (tests/golden/make_golden.py --rows): per-row candidate counts pin any
+    row whose count could drift, not only the batch total."""
+    import json
+    from conftest import GOLDEN
+    ref = json.loads((GOLDEN / "reference_rows_10000000_7500000_7500511.json").read_text())
+    s = searches(ref["limit"])
+    for mode in ("batched", "plain"):
+        got = s.search(ref["first"], ref["last"], mode=mode, rows=True)
+        bad = [(ref["first"] + i, g, w) for i, (g, w) in enumerate(zip(got.row_candidates, ref["candidates"]))
+               if g != w]
+        assert not bad, (mode, bad[:8])
+        assert got.counts["pairs"] == sum(ref["pairs"])
+        assert lines(got.hits) == ref["results"]

@@ -61,3 +61,49 @@ def test_two_replicas_sum_to_the_whole_interval(built):
     assert pairs == whole["pairs"]
     assert cand == whole["candidates"]
     assert hits == sorted(whole["hits"])
+
+
+def _product_rank(rank, world, port, out, limit, first, last):
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    sys.path.insert(0, str(root / "heronian-square-search_gb300"))
+    import hss
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    lo, hi = hss.partition_rows(limit, first, last, world)[rank]
+    with hss.Search(limit, device=0) as s:
+        r = s.search(lo, hi) if lo <= hi else None
+    counts = [r.counts[k] for k in ("pairs", "candidates", "products", "processed")] if r else [0, 0, 0, 0]
+    t = torch.tensor(counts, dtype=torch.int64)
+    dist.all_reduce(t)
+    hits = [None] * world
+    dist.all_gather_object(hits, r.hits if r else [])
+    if rank == 0:
+        out.put((t.tolist(), sorted(h for part in hits for h in part)))
+    dist.destroy_process_group()
+
+
+@pytest.mark.gpu
+def test_two_product_replicas_sum_to_one_search(built):
+    """The replica path through the product: two ranks (processes, one CUDA
+    context each, on the one GPU of this host; their kernels never wait on
+    each other) search their partition_rows shares with hss_search, sum the
+    counters over gloo and gather the hits; the result equals one search of
+    the whole interval.  Root edges 1..100,000 hold both known solutions."""
+    import hss
+    limit, first, last = 100_000, 1, 100_000
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_product_rank, args=(r, 2, port, out, limit, first, last)) for r in range(2)]
+    for p in procs:
+        p.start()
+    (pairs, cand, prod, proc), hits = out.get(timeout=600)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    with hss.Search(limit) as s:
+        whole = s.search(first, last)
+    assert [pairs, cand, prod, proc] == [whole.counts[k] for k in ("pairs", "candidates", "products", "processed")]
+    assert hits == sorted(whole.hits) and len(hits) == 2

@@ -3,15 +3,22 @@ code: a GPU-queue stage and a heavy-root range run on a GB300
 (tests/golden/make_supervisor_fixtures.sh) must be accepted by
 scripts/coverage_audit.py (gpu_complete, heavy_covered), scripts/gpu_queue.py
 (checkpoint_resume) and experiments/heavy/heavy_queue.py (complete), imported
-from the reference checkout.  Skipped where the checkout is absent."""
+from the reference checkout; the results files of the smoke cases and of
+root edges 1..100,000 (tests/golden/make_cli_results.sh) must pass
+scripts/verify.py; and a PROGRESS log or state file damaged on the host must
+be refused by the same code.  Skipped where the checkout is absent."""
 import importlib
 import os
+import subprocess
 import sys
 from pathlib import Path
 
 import pytest
 
-REFERENCE = Path("/root/reference")
+sys.path.insert(0, str(Path(__file__).resolve().parent.parent))
+from __graft_entry__ import reference_checkout  # noqa: E402
+
+REFERENCE = reference_checkout() or Path("reference-checkout-absent")
 FIXTURES = Path(__file__).resolve().parent / "golden" / "supervisor"
 STAGE = (9700000, 9712499)
 HEAVY = (9699328, 9707519)
@@ -70,3 +77,71 @@ def test_heavy_range_accepted_by_coverage_audit_and_heavy_queue():
     queue = _import(REFERENCE / "experiments" / "heavy", "heavy_queue", {"HEAVY_QUEUE_DEADLINE": "4102444800"})
     queue.ROOT = FIXTURES
     assert queue.complete(*HEAVY)
+
+
+@pytest.mark.parametrize("name,lines", [("full5000", 1), ("known2", 1), ("full100k", 2)])
+def test_cli_results_pass_verify_py(name, lines):
+    """scripts/verify.py on the drop-in's results: each line through its
+    verify() (exact bigint Heron, primitivity and area checks) and the whole
+    file through its command line, as scripts/smoke_test.py:60-61 does."""
+    path = FIXTURES / f"{name}-results.txt"
+    if not path.exists():
+        pytest.skip("results fixtures not generated (tests/golden/make_cli_results.sh on a GB300)")
+    rows = [line for line in path.read_text().splitlines() if line.strip()]
+    assert len(rows) == lines
+    verify = _import(REFERENCE / "scripts", "verify")
+    for line in rows:
+        l, m, n, area = map(int, line.split())
+        assert verify.verify(l, m, n, area) == area
+    done = subprocess.run([sys.executable, str(REFERENCE / "scripts" / "verify.py"), str(path)],
+                          capture_output=True, text=True, timeout=120)
+    assert done.returncode == 0, done.stderr
+    assert done.stdout.count("VERIFIED") == lines
+
+
+def _damaged(tmp_path, log_lines, state_text):
+    log = tmp_path / "gpu-0.log"
+    state = tmp_path / "gpu-0-state.txt"
+    log.write_text("".join(x + "\n" for x in log_lines))
+    state.write_text(state_text)
+    return log, state
+
+
+def test_damaged_progress_logs_and_states_are_refused(tmp_path):
+    """Host-side fault injection on the supervisor's inputs: the GB300 stage
+    fixture with a PROGRESS line dropped, a resume altered, the log cut
+    short, or the state truncated is not accepted as complete by
+    coverage_audit.gpu_complete / gpu_queue.checkpoint_resume, and
+    gpu_queue.prepare_checkpoint moves such a pair aside as .unverified
+    (scripts/gpu_queue.py:70-82) instead of resuming from it."""
+    audit = _import(REFERENCE / "scripts", "coverage_audit")
+    queue = _import(REFERENCE / "scripts", "gpu_queue", {"GPU_IDS": "0"})
+    log = (FIXTURES / "gpu-0.log").read_text().splitlines()
+    state = (FIXTURES / "gpu-0-state.txt").read_text()
+    progress = [i for i, line in enumerate(log) if line.startswith("PROGRESS")]
+    bad_resume = list(log)
+    f = bad_resume[progress[3]].split()
+    f[2] = str(int(f[2]) + 1)
+    bad_resume[progress[3]] = " ".join(f)
+    cases = [
+        ("dropped line", [x for i, x in enumerate(log) if i != progress[5]], state),
+        ("altered resume", bad_resume, state),
+        ("cut short", log[:progress[-3]], state),
+        ("truncated state", log, "".join(x + "\n" for x in state.splitlines()[:4])),
+    ]
+    for name, lines, text in cases:
+        case = tmp_path / name.replace(" ", "_")
+        case.mkdir()
+        lpath, spath = _damaged(case, lines, text)
+        assert not audit.gpu_complete(STAGE[0], STAGE[1], spath), name
+        assert queue.checkpoint_resume(STAGE[0], STAGE[1], spath) != STAGE[1] + 1, name
+        queue.prepare_checkpoint(STAGE[0], STAGE[1], spath)
+        kept = sorted(p.name for p in case.iterdir())
+        assert not spath.exists() and any(n.startswith("gpu-0-state.txt.unverified-") for n in kept), (name, kept)
+    # the undamaged pair is accepted and left in place
+    case = tmp_path / "intact"
+    case.mkdir()
+    lpath, spath = _damaged(case, log, state)
+    assert audit.gpu_complete(STAGE[0], STAGE[1], spath)
+    queue.prepare_checkpoint(STAGE[0], STAGE[1], spath)
+    assert spath.exists() and lpath.exists()
