@@ -12,18 +12,31 @@ over that batch through the C ABI (hss_search).  Metric: logical pairs/s.
             items' host-to-device copy from pinned memory, the kernels, and the
             device-to-host read of counters and hits
   plain     the same batch on the plain path (the reference's launch shape)
-  serving   a seeded Poisson stream of interval requests (lengths log-uniform
+  serving   seeded Poisson streams of interval requests (lengths log-uniform
             in [1, 4096] roots, uniform starts) through the serving loop, with
-            p50/p99 latency, against the same requests run one at a time
+            p50/p99 latency and pairs/s, against the same requests one at a
+            time: a rate sweep (10 to 1000 requests/s) at LIMIT 10^5 against
+            the plain and the batched path, and 12 requests at 10/s at
+            LIMIT 10^7 against the batched path
+  uneven    the batched uneven workload (config 4) at LIMIT 10^7: 256 seeded
+            intervals in one hss_search_many call under a CUDA graph with the
+            autotuned kernel variant, every interval checked against its own
+            hss_search, the smallest four also on the plain path
+  config2b  root edges 1..100,000 at LIMIT 10^5 on both paths, candidates
+            against the pinned count
   roofline  integer-op model of the dominant (persistent) kernel against a
             measured INT32 throughput probe; DRAM traffic from an ncu capture
   cpu_baseline  the CPU oracle on a bounded strided sample of the same batch
+            (every row, every 64th m), and configs 1 and 2a end to end
 
 Multi-GPU: replicas.  Rank r searches its own 512-root batch starting at
 7,500,000 + 512 r (weak scaling); there is no collective on the data path.
+Without a launcher, --gpus N starts N local ranks itself (127.0.0.1
+rendezvous) and fails with a message when fewer GPUs are visible.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                  [--no-plain] [--no-cpu] [--no-serving]
+                  [--no-plain] [--no-cpu] [--no-serving] [--no-uneven]
+                  [--no-config2b] [--cpu-sample K] [--intervals P]
   python bench.py --workload uneven [--intervals P] [--steps K] [--warmup W]
 
 --workload uneven times the batched uneven workload instead: a seeded prefix

@@ -413,22 +413,40 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
             const Window w = window(fabsf(d), c);
             und |= g & w.und;
             const bool ok = g & !w.und;
-            // z = S - t and S + t for t = |d|: S -+ d, swapped when d < 0
+            // z = S - t and S + t for t = |d|: S -+ d, swapped when d < 0.
+            // Wide tables: t mod M is taken once (M - (d mod M) when d < 0,
+            // which is M for a multiple of M, still inside two periods) and
+            // both indices come from multiply-adds, off the integer ALU.
             const bool neg = d < 0.f;
             const uint32_t dA = dres % kModA;
-            const uint32_t uA = WIDE ? sA + kModA - dA : sub_mod(sA, dA, kModA);
-            const uint32_t vA = WIDE ? sA + dA : add_mod(sA, dA, kModA);
-            const uint32_t z1 = neg ? vA : uA, z2 = neg ? uA : vA;
+            uint32_t z1, z2;
+            if (WIDE) {
+                const uint32_t tA = neg ? kModA - dA : dA;
+                z1 = imad(tA, 0xFFFFFFFFu, sA + kModA);
+                z2 = imad(tA, 1u, sA);
+            } else {
+                const uint32_t uA = sub_mod(sA, dA, kModA), vA = add_mod(sA, dA, kModA);
+                z1 = neg ? vA : uA;
+                z2 = neg ? uA : vA;
+            }
             const uint32_t m1 = (ok & w.in1) ? tab[kTabA + z1] : 0u;
             const uint32_t m2 = (ok & w.in2) ? tab[kTabA + z2] : 0u;
             pc += ok ? (uint32_t)w.in1 + (uint32_t)w.in2 : 0u;
             pr += (m1 & 1u) + (m2 & 1u);
             // field D of the terms that passed field A
             const uint32_t dD = (oy ? YD : XD) % kModD;
-            const uint32_t uD = WIDE ? sD + kModD - dD : sub_mod(sD, dD, kModD);
-            const uint32_t vD = WIDE ? sD + dD : add_mod(sD, dD, kModD);
-            const uint32_t e1 = (m1 & sel) ? tab_d(tabd, neg ? vD : uD) : 0u;
-            const uint32_t e2 = (m2 & sel) ? tab_d(tabd, neg ? uD : vD) : 0u;
+            uint32_t y1, y2;
+            if (WIDE) {
+                const uint32_t tD = neg ? kModD - dD : dD;
+                y1 = imad(tD, 0xFFFFFFFFu, sD + kModD);
+                y2 = imad(tD, 1u, sD);
+            } else {
+                const uint32_t uD = sub_mod(sD, dD, kModD), vD = add_mod(sD, dD, kModD);
+                y1 = neg ? vD : uD;
+                y2 = neg ? uD : vD;
+            }
+            const uint32_t e1 = (m1 & sel) ? tab_d(tabd, y1) : 0u;
+            const uint32_t e2 = (m2 & sel) ? tab_d(tabd, y2) : 0u;
             f |= (e1 | e2) ? (oy ? kEvDy : kEvDx) : 0u;
         }
         if (!dual) f |= (gx & gy) ? kEvB : 0u;
@@ -1470,17 +1488,44 @@ __global__ void __launch_bounds__(128) merged_setup_kernel(const DeviceCache cac
     }
 }
 
-// Shared-prime pairs of one chunk, a warp per pair, 32 consecutive pairs per
-// warp at a time: the warp reads the pair's descriptor (the next one is
-// loaded while the current pair runs), builds both lists in its shared slice
-// (float and residue products of the prime-power values) and evaluates all
-// (alpha, beta) combinations in lockstep rounds of 32 with a warp event queue.
-constexpr uint32_t kPairWarps = 4;
-__global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const DeviceCache cache, const LaunchBuffers buf,
+// Shared-prime pairs of one chunk, a segment of pairs per warp at a time.  A
+// warp claims blocks of 32 consecutive descriptors from the chunk's cursor
+// (pair sizes vary widely) and stages up to kSegSlots of them in its shared
+// slice; consecutive staged pairs whose lists fit the warp's list arena form
+// a segment.  The segment's lists are built side by side (float and residue
+// products of the prime-power values), and all its (alpha, beta)
+// combinations - the pairs' combination spaces laid end to end - run in
+// lockstep rounds of 32: each lane steps from pair to pair, so rounds stay
+// full across pair boundaries, and the events of every pair of the segment
+// share the warp's queue (drained 32 at a time, one partial drain per
+// segment).  Candidates and mod-16 survivors gather per pair in shared
+// memory; products per pair are counted from the list sizes,
+// 2 na nb - na - nb + 1 (one product per combination with a central value,
+// none for the central pair, which is the analytic all-central product, two
+// otherwise); each pair's counts go to its row once per segment.
+constexpr uint32_t kPairWarps = 8;
+constexpr uint32_t kSegSlots = 8;   // staged pairs (descriptors) per warp
+constexpr uint32_t kSegList = 256;  // list entries of one segment (a pair has at most kWarpListCap)
+static_assert(kSegList >= kWarpListCap, "every warp-sized pair fits a segment alone");
+
+struct SegSlot {
+    uint32_t size;       // na * nb combinations (0: not a warp-sized pair)
+    uint32_t loff;       // first list entry of the pair's side 0 in the arena
+    uint32_t cand, r16;  // counts gathered from the lanes and the event handlers
+};
+
+// Event of a segment: beta index, alpha index, slot, flags (8 bits each).
+__device__ __forceinline__ uint32_t seg_event(uint32_t kb, uint32_t ka, uint32_t k, uint32_t flags) {
+    return kb | (ka << 8) | (k << 16) | (flags << 24);
+}
+
+__global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const DeviceCache cache, const LaunchBuffers buf,
                                                                   uint32_t chunk0) {
-    __shared__ __align__(16) PairDesc s_desc[kPairWarps];
-    __shared__ __align__(16) AlphaHot s_list[kPairWarps][kWarpListCap];
-    __shared__ uint64_t s_queue[kPairWarps][kQueue];
+    constexpr uint32_t kDescWords = sizeof(PairDesc) / 16;
+    __shared__ __align__(16) PairDesc s_desc[kPairWarps][kSegSlots];
+    __shared__ __align__(16) AlphaHot s_list[kPairWarps][kSegList];
+    __shared__ uint32_t s_queue[kPairWarps][kQueue];
+    __shared__ SegSlot s_slot[kPairWarps][kSegSlots];
     // dynamic: root requests, then the wide tables
     extern __shared__ __align__(16) unsigned char s_dyn[];
     RootReq* s_req = reinterpret_cast<RootReq*>(s_dyn);
@@ -1491,84 +1536,153 @@ __global__ void __launch_bounds__(kPairWarps * 32, 4) merged_kernel(const Device
     for (uint32_t i = threadIdx.x; i < kTable2Bytes; i += kPairWarps * 32) s_tab[i] = buf.tables[kTableBytes + i];
     __syncthreads();
     const uint32_t warp = threadIdx.x / 32, lane = threadIdx.x & 31;
-    PairDesc& D = s_desc[warp];
-    uint4* dwords = reinterpret_cast<uint4*>(&D);
-    constexpr uint32_t kDescWords = sizeof(PairDesc) / 16;
+    PairDesc* desc = s_desc[warp];
     AlphaHot* list = s_list[warp];
-    uint64_t* q = s_queue[warp];
+    uint32_t* q = s_queue[warp];
+    SegSlot* slot = s_slot[warp];
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
+    const uint32_t limit = (uint32_t)cache.limit;
     uint32_t qn = 0;
-    // blocks of 32 consecutive pairs from the chunk's cursor (pair sizes vary widely)
     for (;;) {
         uint32_t b0 = 0;
         if (lane == 0) b0 = atomicAdd(buf.desc_next, 32u);
         b0 = __shfl_sync(kFull, b0, 0);
         if (b0 >= n) break;
         const uint32_t b1 = min(b0 + 32, n);
-        uint4 next = lane < kDescWords ? buf.pair_desc[(size_t)b0 * kBigEntryWords + lane] : make_uint4(0, 0, 0, 0);
-        Acc acc{0, 0, 0, 0, 0, 0};
-        uint32_t cur_row = 0xFFFFFFFFu;
-        for (uint32_t i = b0; i < b1; ++i) {
+        for (uint32_t s0 = b0; s0 < b1; s0 += kSegSlots) {
+            const uint32_t ns = min(kSegSlots, b1 - s0);
             __syncwarp();
-            if (lane < kDescWords) dwords[lane] = next;
-            if (i + 1 < b1 && lane < kDescWords) next = buf.pair_desc[(size_t)(i + 1) * kBigEntryWords + lane];
+            for (uint32_t w = lane; w < ns * kDescWords; w += 32)
+                reinterpret_cast<uint4*>(desc)[w] =
+                    buf.pair_desc[(size_t)(s0 + w / kDescWords) * kBigEntryWords + w % kDescWords];
             __syncwarp();
-            if (D.state != 1) continue;
-            if (D.row != cur_row) {
-                if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
-                cur_row = D.row;
-            }
-            if (lane == 0) {
-                acc.prod += 1;
-                acc.cand += D.cc & 1u;
-                acc.r16 += (D.cc >> 1) & 1u;
-            }
-            const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1;
-            for (uint32_t k = lane; k < na + nb; k += 32) {
-                const int side = k < na ? 0 : 1;
-                desc_value_hot(cache, D, side, side ? k - na : k, list[k]);
-            }
-            __syncwarp();
-            const PairCtx c = D.ctx;
-            const uint32_t l = D.l, row = D.row;
-            const uint32_t total = na * nb;
-            // lane's (ka, kb) for k = base + lane, advanced by 32 = q32 nb + r32 per round
-            uint32_t ka = lane / nb, kb = lane - ka * nb;
-            const uint32_t q32 = 32u / nb, r32 = 32u - q32 * nb;
-            auto handle = [&](uint64_t ev, RootReq* slots) -> uint32_t {
-                const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
-                if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
-                const uint2 r = merged_event((uint32_t)(ev >> 40), list[ka], list[na + kb], c, ka, kb, l, row, s_tab,
-                                             kTabD2, (uint32_t)cache.limit, &buf, slots);
-                acc.cand += r.x & 0xFFFFu;
-                acc.r16 += r.y;
-                return r.x >> 16;
-            };
-            auto hit = [&](uint64_t ev, uint32_t tags) {
-                const uint32_t kb = (uint32_t)(ev & 0xFFFFu), ka = (uint32_t)((ev >> 16) & 0xFFFFFFu);
-                push_hits(&buf, tags, ka, kb, l, pair_m(c), row, true);
-            };
-            const bool dual = pair_dual(c);
-            for (uint32_t base = 0; base < total; base += 32) {
-                uint32_t flags = 0;
-                if (base + lane < total) {
-                    const AlphaHot a = list[ka], bh = list[na + kb];
-                    flags = eval_fast<2, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc, dual);
+            for (uint32_t first = 0; first < ns;) {
+                // the segment: staged pairs first .. last - 1 whose lists fit the arena
+                uint32_t entries = 0, combos = 0;
+                if (lane >= first && lane < ns && desc[lane].state == 1) {
+                    const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
+                    entries = na + nb;
+                    combos = na * nb;
                 }
-                if (queue_push(q, qn, flags != 0, make_event(kb, ka, flags)))
-                    drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
-                ka += q32;
-                kb += r32;
-                if (kb >= nb) {
-                    kb -= nb;
-                    ++ka;
+                uint32_t incl = entries;
+#pragma unroll
+                for (int d = 1; d < (int)kSegSlots; d <<= 1) {
+                    const uint32_t t = __shfl_up_sync(kFull, incl, d);
+                    if (lane >= (uint32_t)d) incl += t;
                 }
+                const uint32_t fits = __ballot_sync(kFull, lane >= first && lane < ns && incl <= kSegList);
+                const uint32_t last = first + __popc(fits);
+                uint32_t total = combos;
+                if (lane >= first && lane < last) {
+                    slot[lane].size = combos;
+                    slot[lane].loff = incl - entries;
+                    slot[lane].cand = 0;
+                    slot[lane].r16 = 0;
+                } else {
+                    total = 0;
+                }
+                const uint32_t built = __shfl_sync(kFull, incl, last - 1);
+                total = __reduce_add_sync(kFull, total);
+                __syncwarp();
+                // lists of the segment, entry e of the arena by lane e mod 32
+                for (uint32_t e = lane; e < built; e += 32) {
+                    uint32_t k = first;
+                    while (k + 1 < last && e >= slot[k + 1].loff) ++k;
+                    const uint32_t idx = e - slot[k].loff, na = desc[k].free_count[0] + 1;
+                    desc_value_hot(cache, desc[k], idx < na ? 0 : 1, idx < na ? idx : idx - na, list[e]);
+                }
+                __syncwarp();
+                auto handle = [&](uint32_t ev, RootReq* slots) -> uint32_t {
+                    const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
+                    if (!index_ok(k, last, buf.error_flags) || k < first) return 0u;
+                    const PairDesc& D = desc[k];
+                    const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1, la = slot[k].loff;
+                    if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
+                    const uint2 r = merged_event(ev >> 24, list[la + ka], list[la + na + kb], D.ctx, ka, kb, D.l, D.row,
+                                                 s_tab, kTabD2, limit, &buf, slots);
+                    if (r.x & 0xFFFFu) atomicAdd(&slot[k].cand, r.x & 0xFFFFu);
+                    if (r.y) atomicAdd(&slot[k].r16, r.y);
+                    return r.x >> 16;
+                };
+                auto hit = [&](uint32_t ev, uint32_t tags) {
+                    const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
+                    if (k >= first && k < last)
+                        push_hits(&buf, tags, ka, kb, desc[k].l, pair_m(desc[k].ctx), desc[k].row, true);
+                };
+                // the lane's position: slot k, offset off in it, (ka, kb) = (off / nb, off mod nb)
+                uint32_t k = first, off = lane, size = 0, na = 1, nb = 1, la = 0, ka = 0, kb = 0, q32 = 0, r32 = 0;
+                PairCtx c{};
+                bool dual = false;
+                Acc acc{0, 0, 0, 0, 0, 0};
+                auto enter = [&]() {
+                    while (k < last && off >= slot[k].size) {
+                        off -= slot[k].size;
+                        ++k;
+                    }
+                    if (k < last) {
+                        size = slot[k].size;
+                        na = desc[k].free_count[0] + 1;
+                        nb = desc[k].free_count[1] + 1;
+                        la = slot[k].loff;
+                        ka = off / nb;
+                        kb = off - ka * nb;
+                        q32 = 32u / nb;
+                        r32 = 32u - q32 * nb;
+                        c = desc[k].ctx;
+                        dual = pair_dual(c);
+                    }
+                };
+                enter();
+                for (uint32_t base = 0; base < total; base += 32) {
+                    uint32_t flags = 0;
+                    if (k < last) {
+                        const AlphaHot a = list[la + ka], bh = list[la + na + kb];
+                        flags = eval_fast<2, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc,
+                                                   dual);
+                    }
+                    if (queue_push(q, qn, flags != 0, seg_event(kb, ka, k, flags)))
+                        drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
+                    if (k < last) {
+                        off += 32;
+                        if (off < size) {
+                            ka += q32;
+                            kb += r32;
+                            if (kb >= nb) {
+                                kb -= nb;
+                                ++ka;
+                            }
+                        } else {
+                            if (acc.cand) atomicAdd(&slot[k].cand, acc.cand);
+                            if (acc.r16) atomicAdd(&slot[k].r16, acc.r16);
+                            acc.cand = acc.r16 = 0;
+                            enter();
+                        }
+                    }
+                }
+                while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
+                __syncwarp();
+                // the segment's pairs to their rows
+                if (lane >= first && lane < last && desc[lane].state == 1) {
+                    const PairDesc& D = desc[lane];
+                    const uint64_t pa = D.free_count[0] + 1, pb = D.free_count[1] + 1;
+                    const uint64_t cand = slot[lane].cand + (D.cc & 1u), r16 = slot[lane].r16 + ((D.cc >> 1) & 1u);
+                    const uint64_t prod = 2 * pa * pb - pa - pb + 1;
+                    RowCounts* rc = &buf.rows[D.row];
+                    if (cand) {
+                        atomicAdd(&rc->candidates, (unsigned long long)cand);
+                        atomicAdd(&rc->mcandidates, (unsigned long long)cand);
+                    }
+                    if (r16) {
+                        atomicAdd(&rc->r16, (unsigned long long)r16);
+                        atomicAdd(&rc->mr16, (unsigned long long)r16);
+                    }
+                    atomicAdd(&rc->products, (unsigned long long)prod);
+                    atomicAdd(&rc->mproducts, (unsigned long long)prod);
+                }
+                __syncwarp();
+                first = last;
             }
-            while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
-            __syncwarp();
         }
-        if (cur_row != 0xFFFFFFFFu) flush_acc(acc, &buf.rows[cur_row], true);
-        __syncwarp();
     }
 }
 
@@ -1890,7 +2004,8 @@ cudaError_t launch_merged(const DeviceCache& cache, uint64_t pair_bound, const L
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(buf.desc_next, 0, sizeof(unsigned int), stream);
         if (e != cudaSuccess) return e;
-        merged_kernel<<<ctas, kPairWarps * 32, smem, stream>>>(cache, buf, (uint32_t)c0);
+        // 8-warp CTAs, two per SM: half the grid of the 4-warp kernels
+        merged_kernel<<<(ctas + 1) / 2, kPairWarps * 32, smem, stream>>>(cache, buf, (uint32_t)c0);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         *launches += 2;

@@ -96,8 +96,11 @@ static uint64_t gcd_u64(uint64_t a, uint64_t b) {
     return a;
 }
 
-/* 128-bit value modulo a small modulus (search_v18.cpp:132-138). */
-static uint32_t mod_u128(u128 v, uint32_t p) {
+/* 128-bit value modulo a small modulus (search_v18.cpp:132-138).  Always
+ * inlined: every caller passes a constant modulus, so the compiler replaces
+ * the divisions by multiplications, as the reference's template residue<P>
+ * gets them. */
+static inline __attribute__((always_inline)) uint32_t mod_u128(u128 v, uint32_t p) {
     uint64_t shift = (uint64_t)(((u128)1 << 64) % p);
     uint64_t lo = (uint64_t)v % p, hi = (uint64_t)(v >> 64) % p;
     return (uint32_t)((lo + hi * shift) % p);
@@ -322,9 +325,12 @@ static void test_all(ora_ctx_t *c, gauss_t z) {
  * reference's unrolled depth 1-4 cases enumerate the same products). */
 static void enumerate(ora_ctx_t *c, const ora_term_t *terms, uint32_t count, uint32_t depth,
                       gauss_t z, int free_choice) {
-    if (depth == count) { test_all(c, z); return; }
     const ora_term_t *term = &terms[depth];
     uint32_t last = free_choice ? term->size - 1 : term->central;
+    if (depth + 1 == count) {  /* the last term: the products themselves */
+        for (uint32_t r = 0; r <= last; ++r) test_all(c, g_mul(z, term->values[r]));
+        return;
+    }
     for (uint32_t r = 0; r <= last; ++r)
         enumerate(c, terms, count, depth + 1, g_mul(z, term->values[r]),
                   free_choice || r < term->central);
