@@ -85,7 +85,7 @@ SWEEP_LIMIT = 100_000    # rate sweep: requests of milliseconds, so the rates sp
 SWEEP_RATES = (10.0, 30.0, 100.0, 300.0, 1000.0)
 SWEEP_WINDOW_S = 2.0     # requests per rate: rate x window, within [MIN, MAX]
 SWEEP_MIN_REQUESTS = 20
-SWEEP_MAX_REQUESTS = 200
+SWEEP_MAX_REQUESTS = 100
 
 # batched uneven workload (config 4)
 UNEVEN_SEED = 4

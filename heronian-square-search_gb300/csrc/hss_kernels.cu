@@ -457,9 +457,14 @@ __device__ __forceinline__ uint32_t eval_fast(const AlphaHot& a, float br, float
     }
     acc.cand += cnt;
     acc.r16 += r16;
-    acc.prod += (ca | cb) ? ((ca & cb) ? 0u : 1u) : 2u;
     return flags;
 }
+
+// Gaussian products of a pair whose two sides have na and nb values (each
+// list or segment ending with its central value): two per combination of
+// non-central values (alpha beta and alpha conj(beta)), one when exactly one
+// value is central, and the all-central product, 2 na nb - na - nb + 1.
+__device__ __forceinline__ uint32_t pair_products(uint32_t na, uint32_t nb) { return 2 * na * nb - na - nb + 1; }
 
 // A possible hit needs some n in [m, N] with n^4 = z.  From z's float bounds
 // (|error| below sf 2^-22 + eps + |z| 2^-22) take the window of n with n^4
@@ -864,6 +869,19 @@ __device__ __forceinline__ void push_merged(const LaunchBuffers& buf, uint32_t l
         atomicOr(buf.error_flags, 1u);
 }
 
+// Per-lane flush of the counters into a row's counters (64-bit atomics): for
+// kernels whose threads each cover so much of a row that a warp's 32-bit sum
+// could pass 2^32.
+__device__ __forceinline__ void flush_acc_lanes(Acc& acc, RowCounts* rc) {
+    if (acc.cand) atomicAdd(&rc->candidates, (unsigned long long)acc.cand);
+    if (acc.r16) atomicAdd(&rc->r16, (unsigned long long)acc.r16);
+    if (acc.prod) atomicAdd(&rc->products, (unsigned long long)acc.prod);
+    if (acc.exact) atomicAdd(&rc->exact, (unsigned long long)acc.exact);
+    if (acc.processed) atomicAdd(&rc->processed, (unsigned long long)acc.processed);
+    if (acc.merged) atomicAdd(&rc->merged, (unsigned long long)acc.merged);
+    acc = Acc{0, 0, 0, 0, 0, 0};
+}
+
 // Warp-level reduction of the per-thread counters into a row's counters;
 // `shared_prime` also books them as work of the shared-prime kernels.
 __device__ __forceinline__ void flush_acc(Acc& acc, RowCounts* rc, bool shared_prime = false) {
@@ -1119,7 +1137,7 @@ __global__ void __launch_bounds__(NT, MINB) batched_kernel(const DeviceCache cac
                         cnt_single[u] = seg1 - seg0;
                     }
                     acc.processed += 1;
-                    acc.prod += 1;
+                    acc.prod += pair_products(na, seg1 - seg0);
                     acc.cand += cc_c;
                     acc.r16 += cc_r;
                 } else if (kind == kMerged) {
@@ -1175,7 +1193,7 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
         }
         uint32_t cc_c, cc_r;
         const PairCtx c = make_ctx(R, m, cc_c, cc_r);
-        acc.prod += 1;
+        acc.prod += pair_products(na, s1 - s0);
         acc.cand += cc_c;
         acc.r16 += cc_r;
         for (uint32_t j = s0; j < s1; ++j) {
@@ -1191,7 +1209,7 @@ __global__ void __launch_bounds__(kPlainThreads, 4) plain_kernel(const DeviceCac
             }
         }
     }
-    flush_acc(acc, &buf.rows[row]);
+    flush_acc_lanes(acc, &buf.rows[row]);
 }
 
 // ------------------------------------------------------------- merged kernels
@@ -1551,9 +1569,21 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
         const uint32_t b1 = min(b0 + 32, n);
         for (uint32_t s0 = b0; s0 < b1; s0 += kSegSlots) {
             const uint32_t ns = min(kSegSlots, b1 - s0);
+            // staged with the dual pairs (both orientations live) first, so
+            // that a segment's rounds mix dual and single-orientation lanes
+            // at one boundary at most (word 2 of a descriptor holds ctx.m,
+            // whose bit 31 is the dual flag)
+            const bool dual_i =
+                lane < ns && (buf.pair_desc[(size_t)(s0 + lane) * kBigEntryWords + 2].w >> 31) != 0;
+            const uint32_t dmask = __ballot_sync(kFull, dual_i), vmask = (1u << ns) - 1u;
+            auto dest = [&](uint32_t i) {
+                const uint32_t below = (1u << i) - 1u;
+                return ((dmask >> i) & 1u) ? (uint32_t)__popc(dmask & below)
+                                           : (uint32_t)(__popc(dmask) + __popc(~dmask & vmask & below));
+            };
             __syncwarp();
             for (uint32_t w = lane; w < ns * kDescWords; w += 32)
-                reinterpret_cast<uint4*>(desc)[w] =
+                reinterpret_cast<uint4*>(desc)[dest(w / kDescWords) * kDescWords + w % kDescWords] =
                     buf.pair_desc[(size_t)(s0 + w / kDescWords) * kBigEntryWords + w % kDescWords];
             __syncwarp();
             for (uint32_t first = 0; first < ns;) {
@@ -1666,7 +1696,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
                     const PairDesc& D = desc[lane];
                     const uint64_t pa = D.free_count[0] + 1, pb = D.free_count[1] + 1;
                     const uint64_t cand = slot[lane].cand + (D.cc & 1u), r16 = slot[lane].r16 + ((D.cc >> 1) & 1u);
-                    const uint64_t prod = 2 * pa * pb - pa - pb + 1;
+                    const uint64_t prod = pair_products((uint32_t)pa, (uint32_t)pb);
                     RowCounts* rc = &buf.rows[D.row];
                     if (cand) {
                         atomicAdd(&rc->candidates, (unsigned long long)cand);
@@ -1728,7 +1758,7 @@ __global__ void __launch_bounds__(kMergedThreads, 4) merged_big_kernel(const Dev
         __syncthreads();
         Acc acc{0, 0, 0, 0, 0, 0};
         if (threadIdx.x == 0) {
-            acc.prod += 1;
+            acc.prod += pair_products(na, nb);
             acc.cand += D.cc & 1u;
             acc.r16 += (D.cc >> 1) & 1u;
         }
