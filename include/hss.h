@@ -220,8 +220,14 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
  * Requests are queued by hss_submit and advanced by a background loop that
  * launches waves of batched work; each wave takes a bounded slice of every
  * admitted request, so requests that arrive while others run join at the
- * next wave.  Admission is capped by free device memory and by
- * max_active.  Results are the same as hss_search on the same interval. */
+ * next wave.  Waves alternate between two launch lanes (a stream and launch
+ * buffers each), so one runs while the previous one is harvested.  Every
+ * admitted request keeps its per-row counters in a device arena sized at
+ * hss_serve_start (hss_opts.serve_state_kb, else 1/16 of free device memory
+ * up to 256 MiB; 80 bytes per root row): a request is admitted when a slot
+ * (max_active) and room for its rows are free, and hss_submit refuses one
+ * larger than the whole arena (HSS_ERR_MEMORY).  Results are the same as
+ * hss_search on the same interval.  No counterpart in the reference. */
 typedef struct {
     uint64_t first, last;
     uint64_t submitted_ns;  /* CLOCK_MONOTONIC at submit */
