@@ -1215,10 +1215,19 @@ void serve_loop(hss_t* h) {
                 r->next_row = r->first;
                 active.push_back(r);
             }
-            // the wave: a share of the pair budget for every admitted request, oldest first
+            // The wave: the oldest admitted request with rows left takes the
+            // pair budget, every younger one a single row.  Large requests
+            // then finish in arrival order, as one at a time would, while
+            // every newcomer advances in every wave, so short requests end
+            // within a few waves instead of waiting behind the large ones.
+            std::vector<Request*> order;
+            for (Request* r : active)
+                if (r->next_row <= r->last) order.push_back(r);
+            std::sort(order.begin(), order.end(), [](const Request* x, const Request* y) { return x->id < y->id; });
             const uint64_t budget = (uint64_t)h->wave_items << 20;
-            const uint64_t share = std::max<uint64_t>(budget / std::max<size_t>(active.size(), 1), 1);
-            for (Request* r : active) {
+            for (size_t i = 0; i < order.size(); ++i) {
+                Request* r = order[i];
+                const uint64_t share = i == 0 ? budget : 0;
                 uint64_t taken = 0;
                 while (r->next_row <= r->last && (taken == 0 || taken + (h->limit - r->next_row + 1) <= share)) {
                     taken += h->limit - r->next_row + 1;

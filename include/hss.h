@@ -218,9 +218,10 @@ int hss_search_many(hss_t* h, const uint64_t* firsts, const uint64_t* lasts, uin
 
 /* ---- serving: continuous admission of interval requests ----
  * Requests are queued by hss_submit and advanced by a background loop that
- * launches waves of batched work; each wave takes a bounded slice of every
- * admitted request, so requests that arrive while others run join at the
- * next wave.  Waves alternate between two launch lanes (a stream and launch
+ * launches waves of batched work: each wave takes wave_mpairs x 2^20 logical
+ * pairs from the oldest admitted request and one root row from every younger
+ * one, so requests that arrive while others run join at the next wave, short
+ * ones finish within a few waves, and large ones finish in arrival order.  Waves alternate between two launch lanes (a stream and launch
  * buffers each), so one runs while the previous one is harvested.  Every
  * admitted request keeps its per-row counters in a device arena sized at
  * hss_serve_start (hss_opts.serve_state_kb, else 1/16 of free device memory
