@@ -15,7 +15,6 @@
 
 #include <algorithm>
 #include <array>
-#include <atomic>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -46,8 +45,6 @@ constexpr uint32_t kDescChunk = 1u << 22;       // shared-prime pairs set up per
 }  // namespace
 
 namespace {
-
-std::mutex g_err_mu;
 
 int fail(hss_t* h, int status, const std::string& msg) {
     if (h) h->err = msg;

@@ -257,7 +257,7 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     uint32_t top = 0;
     for (uint32_t r = rows; r-- > 0;)
         g_stack[top++] = Piece{r, (uint32_t)(first + r), (uint32_t)(h->limit + 1)};
-    uint32_t max_group = kNaRows, nh = 0, groups = 0;
+    uint32_t max_group = kNaRows, nh = 0;
     uint64_t found = 0, h2d = rows * sizeof(RowInfo), d2h = 0;
     double ms = 0;
     uint32_t launches = 0;
@@ -301,7 +301,6 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
         }
         if (s) return s;
         top = lo;
-        ++groups;
         ms += res.ms;
         launches += res.launches;
         h2d += res.h2d;
@@ -340,7 +339,6 @@ int run(hss_t* h, uint64_t first, uint64_t last, hss_counts* out, hss_hit* hits,
     out->graph_launches = 0;
     out->h2d_bytes = h2d;
     out->d2h_bytes = d2h;
-    (void)groups;
     for (uint32_t i = 0; i < unique && i < hit_cap && hits; ++i) {
         hits[i].l = g_host_hits[i].l;
         hits[i].m = g_host_hits[i].m;
