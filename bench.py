@@ -517,9 +517,9 @@ def our_arm(args, rank, world, local_rank):
         t = json.loads(TRAFFIC.read_text())
         traffic = t.get("batched_kernel_bytes_per_launch")
         if traffic and PEAKS.exists():
-            # the measured case's DRAM bytes per logical pair, over this step's pairs
-            mc = t["measured_case"]
-            gbs = mc["bytes"] / mc["pairs"] * c["pairs"] / (main_ms * 1e-3) / 1e9
+            # the persistent kernel's DRAM bytes of this batch (every launch of
+            # it, captured on the batch itself) over its device time
+            gbs = t["batch_bytes"] / (main_ms * 1e-3) / 1e9
             peak_gbs = json.loads(PEAKS.read_text()).get("hbm_gbs")
             hbm = {"achieved_gbs": gbs, "peak_gbs": peak_gbs, "frac": gbs / peak_gbs if peak_gbs else None,
                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
