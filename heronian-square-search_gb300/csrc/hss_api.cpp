@@ -38,8 +38,8 @@ constexpr uint32_t kDefaultItemTarget = 1u << 22;
 constexpr uint32_t kTileCap = 16384;           // largest m-range of one item
 constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
-constexpr uint64_t kMergedCap = 48ull << 20;   // shared-prime queue entries
-constexpr uint32_t kDescChunk = 1u << 22;       // shared-prime pairs set up per chunk (192 bytes each: 768 MB)
+constexpr uint64_t kMergedCap = 96ull << 20;   // shared-prime queue entries
+constexpr uint32_t kDescChunk = 1u << 24;       // shared-prime pairs set up per chunk (192 bytes each: 3 GB)
 
 
 }  // namespace
