@@ -34,7 +34,7 @@ namespace {
 
 constexpr uint32_t kDefaultHitCap = 4096;      // gpu_search_v42.cu:177-178
 constexpr uint32_t kPlainBatch = 512;          // gpu_search_v42.cu:457
-constexpr uint32_t kDefaultItemTarget = 1u << 22;
+constexpr uint32_t kDefaultItemTarget = 1u << 23;
 constexpr uint32_t kTileCap = 16384;           // largest m-range of one item
 constexpr uint32_t kTileMin = 32;
 constexpr uint32_t kBucketShift = 10;          // item ordering granularity in m
@@ -883,7 +883,7 @@ int hss_autotune(hss_t* h, uint64_t first, uint64_t last, hss_opts* best, hss_tu
                  uint32_t max_trials, uint32_t* ntrials) {
     if (!h) return HSS_ERR_ARGUMENT;
     static const uint32_t kVariants[][2] = {{128, 4}, {128, 6}, {256, 2}, {256, 3}, {512, 1}};
-    static const uint32_t kTargets[] = {1u << 21, 1u << 22, 1u << 23};
+    static const uint32_t kTargets[] = {1u << 21, 1u << 22, 1u << 23, 1u << 24, 1u << 25};
     const hss_opts saved = h->opts;
     hss_opts chosen = saved;
     float best_ms = 0;

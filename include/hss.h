@@ -53,7 +53,7 @@ typedef struct {
                                  gpu_search_v42.cu:177-178) */
     uint32_t block_threads;   /* batched CTA size: 128, 256 or 512 (0: 256) */
     uint32_t item_target;     /* batched item weight in alpha*beta evaluations
-                                 (0: 1<<22) */
+                                 (0: 1<<23) */
     uint32_t ctas_per_sm;     /* batched kernel variant: minimum CTAs per SM it is
                                  compiled for (128 threads: 4 or 6; 256: 2 or 3;
                                  512: 1); 0 picks 4 / 2 / 1 */
