@@ -146,31 +146,44 @@ int ensure_merged(hss_t* h, uint64_t n) {
     return HSS_OK;
 }
 
-// A launch group whose exact work outgrew the queue is incomplete: the queue
-// is enlarged 4x (up to 2^28 items) and the caller runs the whole call again.
-int grow_exact(hss_t* h) {
-    if (!h->exact_overflow) return HSS_ERR_OVERFLOW;
-    h->exact_overflow = false;
-    const uint64_t cap = (uint64_t)h->exact_cap * 4;
-    if (cap > (1ull << 28)) return HSS_ERR_OVERFLOW;
+// A launch group whose exact work outgrew the exact queue, or whose big
+// shared-prime pairs outgrew the big-pair queue, is incomplete: the queue
+// that overflowed is enlarged 4x (exact: up to 2^28 items; big pairs: up to
+// 2^24 descriptors of 192 bytes) and the caller runs the whole call again.
+int grow_overflowed(hss_t* h) {
+    if (!h->exact_overflow && !h->big_overflow) return HSS_ERR_OVERFLOW;
     HSS_CUDA(h, cudaStreamSynchronize(h->stream));
-    device_free(h, h->d_exact);
-    h->d_exact = nullptr;
-    int s = device_alloc(h, &h->d_exact, (size_t)cap);
-    if (s) return s;
-    h->exact_cap = (uint32_t)cap;
+    if (h->exact_overflow) {
+        h->exact_overflow = false;
+        const uint64_t cap = (uint64_t)h->exact_cap * 4;
+        if (cap > (1ull << 28)) return HSS_ERR_OVERFLOW;
+        device_free(h, h->d_exact);
+        h->d_exact = nullptr;
+        if (int s = device_alloc(h, &h->d_exact, (size_t)cap)) return s;
+        h->exact_cap = (uint32_t)cap;
+    }
+    if (h->big_overflow) {
+        h->big_overflow = false;
+        const uint64_t cap = (uint64_t)h->big_cap * 4;
+        if (cap > (1ull << 24)) return HSS_ERR_OVERFLOW;
+        device_free(h, h->d_big);
+        h->d_big = nullptr;
+        if (int s = device_alloc(h, &h->d_big, (size_t)cap * kBigEntryWords)) return s;
+        h->big_cap = (uint32_t)cap;
+    }
     return HSS_OK;
 }
 
-// Runs `call` again after enlarging the exact queue when it overflowed (the
-// queue grows 4x per rerun, up to 2^28 items; h->call_reruns counts them).
+// Runs `call` again after enlarging the queue that overflowed (4x per rerun;
+// h->call_reruns counts the reruns).
 template <class Call>
 int with_exact_retry(hss_t* h, Call call) {
     for (uint32_t attempt = 0;; ++attempt) {
-        h->exact_overflow = false;
+        h->exact_overflow = h->big_overflow = false;
         h->call_reruns = attempt;
         const int s = call();
-        if (s == HSS_ERR_OVERFLOW && h->exact_overflow && grow_exact(h) == HSS_OK) continue;
+        if (s == HSS_ERR_OVERFLOW && (h->exact_overflow || h->big_overflow) && grow_overflowed(h) == HSS_OK)
+            continue;
         return s;
     }
 }
@@ -517,11 +530,12 @@ int end_call(hss_t* h, size_t rows, double* ms, std::vector<DevHit>* hits, uint3
     h->d2h_bytes += rows * sizeof(RowCounts) + sizeof ctrl;
     if (ctrl[3] & 1u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime queue over capacity");
     if (ctrl[3] & 2u) return fail(h, HSS_ERR_OVERFLOW, "shared-prime pair exceeds the list capacity");
-    if (ctrl[3] & 4u) {
-        h->exact_overflow = true;
-        return fail(h, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+    if (ctrl[3] & 12u) {
+        h->exact_overflow = (ctrl[3] & 4u) != 0;
+        h->big_overflow = (ctrl[3] & 8u) != 0;
+        return fail(h, HSS_ERR_OVERFLOW, "exact work or big-pair queue over capacity");
     }
-    if (ctrl[3] & ~7u) return fail(h, HSS_ERR_OVERFLOW, "a device index check failed (an event index out of range)");
+    if (ctrl[3] & ~15u) return fail(h, HSS_ERR_OVERFLOW, "a device index check failed (an event index out of range)");
     uint32_t nh = std::min(ctrl[0], h->hit_cap);
     hits->resize(nh);
     if (nh) HSS_CUDA(h, cudaMemcpy(hits->data(), h->d_hits, nh * sizeof(DevHit), cudaMemcpyDeviceToHost));
@@ -1096,14 +1110,17 @@ int launch_wave(hss_t* h, hss_t* lane, const Wave& w) {
 }
 
 // Waits for a lane's wave and collects its hits and device time; a wave whose
-// exact-work queue overflowed runs again (grown queue) before it counts.
+// exact-work or big-pair queue overflowed runs again (grown queue) before it
+// counts.
 int finish_wave(hss_t* h, hss_t* lane, const Wave& w, std::vector<DevHit>* hits, double* ms) {
     for (uint32_t attempt = 0;; ++attempt) {
         HSS_CUDA(lane, cudaStreamSynchronize(lane->stream));
         const unsigned int* ctrl = lane->h_ctrl;
-        if (ctrl[3] & 4u) {
-            lane->exact_overflow = true;
-            if (grow_exact(lane) != HSS_OK) return fail(lane, HSS_ERR_OVERFLOW, "exact work queue over capacity");
+        if ((ctrl[3] & 12u) && !(ctrl[3] & 3u)) {
+            lane->exact_overflow = (ctrl[3] & 4u) != 0;
+            lane->big_overflow = (ctrl[3] & 8u) != 0;
+            if (grow_overflowed(lane) != HSS_OK)
+                return fail(lane, HSS_ERR_OVERFLOW, "exact work or big-pair queue over capacity");
             if (int s = launch_wave(h, lane, w)) return s;
             continue;
         }

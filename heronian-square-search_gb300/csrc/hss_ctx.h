@@ -88,6 +88,7 @@ struct hss_ctx {
     hss::ExactItem* d_exact = nullptr;    // exact work queue
     uint32_t exact_cap = 0;
     bool exact_overflow = false;          // the last launch group outgrew it
+    bool big_overflow = false;            // ... or outgrew the big-pair queue
     uint32_t call_reruns = 0;             // reruns of the current call after growing it
     uint4* d_merged = nullptr;
     uint32_t merged_cap = 0;

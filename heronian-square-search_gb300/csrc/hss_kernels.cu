@@ -1496,7 +1496,7 @@ __global__ void __launch_bounds__(128) merged_setup_kernel(const DeviceCache cac
                 uint4* dst = buf.big_queue + (size_t)idx * kBigEntryWords;
                 for (uint32_t w = 0; w < sizeof(PairDesc) / 16; ++w) dst[w] = src[w];
             } else {
-                atomicOr(buf.error_flags, 2u);
+                atomicOr(buf.error_flags, 8u);  // the big-pair queue is full: the host grows it and reruns
             }
         } else if (D.state == 3) {
             atomicOr(buf.error_flags, 2u);

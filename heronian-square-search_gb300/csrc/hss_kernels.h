@@ -66,7 +66,8 @@ struct LaunchBuffers {
     unsigned int* merged_count; // entries appended (may exceed merged_cap)
     uint32_t merged_cap;
     unsigned int* next_item;    // work-queue cursor of the batched kernel
-    unsigned int* error_flags;  // bit 0: shared-prime queue full; 1: pair lists over capacity; 2: exact queue full
+    unsigned int* error_flags;  // bit 0: shared-prime queue full; 1: pair lists over capacity; 2: exact queue
+                                // full; 3: big-pair queue full; 8 (0x100): an event index check failed
     uint4* big_queue;           // shared-prime pairs too big for one warp's lists: kBigEntryWords
                                 // words each (the pair's descriptor, written by the set-up kernel)
     unsigned int* big_count;

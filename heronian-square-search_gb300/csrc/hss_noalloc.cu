@@ -207,7 +207,7 @@ int run_group(hss_t* h, unsigned char* base, uint32_t rows, uint32_t lo, uint32_
     NA_CUDA(cudaMemcpyAsync(g_host_ctrl, ctrl, sizeof g_host_ctrl, cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaMemcpyAsync(g_host_counts, b.rows, rows * sizeof(RowCounts), cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaStreamSynchronize(st));
-    if (g_host_ctrl[3] & ~7u) return fail(h, HSS_ERR_CUDA, "hss_search_noalloc: a device index check failed");
+    if (g_host_ctrl[3] & ~15u) return fail(h, HSS_ERR_CUDA, "hss_search_noalloc: a device index check failed");
     if (g_host_ctrl[3]) return fail(h, HSS_ERR_OVERFLOW, "hss_search_noalloc: a scratch queue overflowed");
     const uint32_t group_hits = std::min(g_host_ctrl[0], kNaHits);
     const uint32_t room = kNaHits - *nh;

@@ -98,7 +98,7 @@ typedef struct {
     uint32_t launches;           /* kernels launched by the call */
     uint32_t graph_launches;     /* CUDA graph launches of the call (opts.use_graph) */
     uint32_t reruns;             /* times the call ran again after growing the
-                                    exact-work queue */
+                                    exact-work or big-pair queue */
     uint32_t reserved;
 } hss_counts;
 
