@@ -1530,7 +1530,18 @@ struct SegSlot {
     uint32_t size;       // na * nb combinations (0: not a warp-sized pair)
     uint32_t loff;       // first list entry of the pair's side 0 in the arena
     uint32_t cand, r16;  // counts gathered from the lanes and the event handlers
+    uint32_t nab;        // na | nb << 16
+    uint32_t step;       // ceil(2^16 / nb) | (32 / nb) << 17 | (32 mod nb) << 23
 };
+
+// A lane entering a pair of the segment does so at an offset below 32 (it
+// stepped at most 32 past the previous pair's end), so off / nb is taken as
+// off * ceil(2^16 / nb) >> 16, exact for off < 32 and nb < 2^8: the error term
+// off * (ceil(2^16 / nb) - 2^16 / nb) / 2^16 stays below 32 / 2^16, less than the
+// gap 1/nb between off / nb and the next integer.
+__device__ __forceinline__ uint32_t seg_step(uint32_t nb) {
+    return (65536u + nb - 1) / nb | (32u / nb) << 17 | (32u % nb) << 23;
+}
 
 // Event of a segment: beta index, alpha index, slot, flags (8 bits each).
 __device__ __forceinline__ uint32_t seg_event(uint32_t kb, uint32_t ka, uint32_t k, uint32_t flags) {
@@ -1608,6 +1619,11 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
                     slot[lane].loff = incl - entries;
                     slot[lane].cand = 0;
                     slot[lane].r16 = 0;
+                    if (combos) {
+                        const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
+                        slot[lane].nab = na | nb << 16;
+                        slot[lane].step = seg_step(nb);
+                    }
                 } else {
                     total = 0;
                 }
@@ -1650,14 +1666,15 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
                         ++k;
                     }
                     if (k < last) {
+                        const uint32_t nab = slot[k].nab, st = slot[k].step;
                         size = slot[k].size;
-                        na = desc[k].free_count[0] + 1;
-                        nb = desc[k].free_count[1] + 1;
+                        na = nab & 0xFFFFu;
+                        nb = nab >> 16;
                         la = slot[k].loff;
-                        ka = off / nb;
+                        ka = (off * (st & 0x1FFFFu)) >> 16;  // off < 32 here (see seg_step)
                         kb = off - ka * nb;
-                        q32 = 32u / nb;
-                        r32 = 32u - q32 * nb;
+                        q32 = (st >> 17) & 63u;
+                        r32 = st >> 23;
                         c = desc[k].ctx;
                         dual = pair_dual(c);
                     }
