@@ -794,8 +794,9 @@ __device__ __forceinline__ uint32_t classify(const RowInfo& R, uint32_t m, uint3
 // nonzero area is D = 0, 4A = 2 l^2 m^2 (counted when the window contains 0;
 // z = l^4 + m^4 is never a fourth power).
 // eps_scale: 2^-20 for values read from the cache (float coordinates within
-// 2^-24 relative, products within 4 * 2^-24 of |z|), 2^-16 for shared-prime
-// lists multiplied out in float (at most 16 factors: within 71 * 2^-24).
+// 2^-24 relative, products within 4.9 * 2^-24 of |z|); for shared-prime lists
+// multiplied out in float, (12 + 8 K) 2^-24 for a pair whose two groups hold
+// K terms (see shared_prime_eps_scale).
 __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16,
                            float eps_scale = 0x1p-20f) {
     uint64_t m2 = m * m;
@@ -1402,6 +1403,20 @@ struct __align__(16) PairDesc {
 static_assert(sizeof(PairDesc) <= kBigEntryWords * 16 && sizeof(PairDesc) % 16 == 0,
               "a descriptor fits one big-queue entry");
 
+// Error bound of a shared-prime pair's float products, relative to |z|, with
+// u = 2^-24.  A float complex product x v (with or without fused multiply-
+// adds) is within 2 sqrt(2) u |x| |v| of the product of its float inputs, as
+// |x_re v_re| + |x_im v_im| <= |x| |v| for each component; an input with
+// relative error e_x adds e_x |x| |v|.  A list value is the group's scale
+// (within 3 u: an i128 rounded to float) times one prime-power value per term
+// of the group (each within u, correctly rounded), so it is within
+// 3 u + 3.83 k u for k terms; the filter loop's product alpha beta adds the
+// two values' errors and 2.83 u.  For K = k0 + k1 terms that is at most
+// (5.83 + 3.83 K) u; the bound used, (12 + 8 K) u, keeps a factor 2 (and is
+// never looser than the 2^-16 once used for every pair, as K <= 20).  Every
+// window decision and root window of the pair is taken against it.
+__device__ __forceinline__ float shared_prime_eps_scale(uint32_t K) { return (float)(12 + 8 * K) * 0x1p-24f; }
+
 __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, PairDesc& D, uint32_t cap) {
     MergedShared S;
     merged_setup(cache, R, q, S, cap);
@@ -1422,7 +1437,7 @@ __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint
     D.scale_f = S.g[0].scale_f;
     D.scale_res = S.g[0].scale_res;
     uint32_t cc_c, cc_r;
-    D.ctx = make_ctx(R, q.y, cc_c, cc_r, 0x1p-16f);
+    D.ctx = make_ctx(R, q.y, cc_c, cc_r, shared_prime_eps_scale(S.g[0].count + S.g[1].count));
     D.cc = (uint8_t)(cc_c | (cc_r << 1));
 }
 
