@@ -184,3 +184,42 @@ def test_signal_stops_at_a_batch_boundary(built, tmp_path, sig):
     assert progress_chain_ok(r2.stdout, v["resume"], last)
     with hss.Search(limit) as s:
         assert c1 + v2["candidates"] == s.search(first, last).counts["candidates"]
+
+
+@pytest.mark.gpu
+def test_queue_launch_found_by_ps(built, tmp_path):
+    """Launched the way scripts/gpu_queue.py:174-191 launches it (ROOT/gpu_search_v42,
+    argv LIMIT FIRST LAST RESULTS GPU STATE, cwd ROOT, stdout and stderr into
+    the log), the running search is what gpu_queue.running finds
+    (scripts/gpu_queue.py:85-98): `ps -C gpu_search_v42 -o pid=,args=` lists
+    it with exactly 8 fields, field 6 the GPU and field 7 a state file named
+    gpu-<GPU>...; SIGTERM then ends it at a batch boundary with exit 0."""
+    import signal
+    import time
+    (tmp_path / "gpu_search_v42").symlink_to(BINARY)
+    first, last = 9_800_000, 9_812_499  # GPU 0's interval of stage "a"
+    state, results = tmp_path / "gpu-0a-state.txt", tmp_path / "gpu-0a-results.txt"
+    with open(tmp_path / "gpu-0a.log", "a") as log:
+        p = subprocess.Popen([str(tmp_path / "gpu_search_v42"), "10000000", str(first), str(last), str(results),
+                              "0", str(state)], cwd=tmp_path, stdout=log, stderr=subprocess.STDOUT)
+    found = None
+    try:
+        # looked up mid-run (after its first batch), as the queue's 5 s poll sees it
+        deadline = time.time() + 300
+        while p.poll() is None and time.time() < deadline and "PROGRESS" not in (tmp_path / "gpu-0a.log").read_text():
+            time.sleep(0.005)
+        out = subprocess.run(["ps", "-C", "gpu_search_v42", "-o", "pid=,args="], text=True,
+                             capture_output=True).stdout
+        found = next((l.split() for l in out.splitlines() if l.split()[:1] == [str(p.pid)]), None)
+    finally:
+        if p.poll() is None:
+            p.send_signal(signal.SIGTERM)
+        assert p.wait(timeout=600) == 0
+    assert found is not None
+    assert len(found) == 8
+    assert found[2:5] == ["10000000", str(first), str(last)]
+    assert Path(found[5]).name == results.name
+    assert found[6] == "0" and Path(found[7]).name.startswith("gpu-0")
+    v = read_state(state)
+    assert v["begin"] == first
+    assert (v["resume"] - first) % 512 == 0 or v["resume"] == last + 1

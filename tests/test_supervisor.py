@@ -5,10 +5,15 @@ scripts/coverage_audit.py (gpu_complete, heavy_covered), scripts/gpu_queue.py
 (checkpoint_resume) and experiments/heavy/heavy_queue.py (complete), imported
 from the reference checkout; the results files of the smoke cases and of
 root edges 1..100,000 (tests/golden/make_cli_results.sh) must pass
-scripts/verify.py; and a PROGRESS log or state file damaged on the host must
-be refused by the same code.  Skipped where the checkout is absent."""
+scripts/verify.py; a PROGRESS log or state file damaged on the host must
+be refused by the same code; and the reference's scripts/gpu_follow.py and
+scripts/gpu_queue.py, run as processes, must take the checkpoints of two
+GPU-queue stages that the drop-in wrote on a GB300
+(tests/golden/make_follow_fixtures.py) to the end of the stage chain.
+Skipped where the checkout is absent."""
 import importlib
 import os
+import shutil
 import subprocess
 import sys
 from pathlib import Path
@@ -145,3 +150,95 @@ def test_damaged_progress_logs_and_states_are_refused(tmp_path):
     assert audit.gpu_complete(STAGE[0], STAGE[1], spath)
     queue.prepare_checkpoint(STAGE[0], STAGE[1], spath)
     assert spath.exists() and lpath.exists()
+
+
+FOLLOW = FIXTURES / "follow"
+FOLLOW_STAGES = {"a": (9800000, 9812499), "b": (9600000, 9612499)}
+
+
+def _queue_root(tmp_path):
+    """A queue ROOT holding the reference's scripts (copied: they take ROOT
+    from their own location, scripts/gpu_queue.py:16) and the files that the
+    drop-in wrote on a GB300 for GPU 0's intervals of stages a and b
+    (tests/golden/make_follow_fixtures.py)."""
+    if not (FOLLOW / "gpu-0b-state.txt").exists():
+        pytest.skip("follow fixtures not generated (tests/golden/make_follow_fixtures.py on a GB300)")
+    root = tmp_path / "root"
+    (root / "scripts").mkdir(parents=True)
+    for name in ("gpu_follow.py", "gpu_queue.py", "gpu_stages.py", "verify.py"):
+        shutil.copy(REFERENCE / "scripts" / name, root / "scripts" / name)
+    for f in FOLLOW.iterdir():
+        if f.name.startswith("gpu-0"):
+            shutil.copy(f, root / f.name)
+    return root
+
+
+def _run_script(root, *args, timeout=600):
+    env = dict(os.environ, GPU_IDS="0", PYTHONDONTWRITEBYTECODE="1")
+    return subprocess.run([sys.executable, *map(str, args)], cwd=root, env=env, capture_output=True, text=True,
+                          timeout=timeout)
+
+
+def test_follow_fixtures_were_launched_as_the_queue_launches():
+    """What the GB300 run recorded while stage a ran: `ps -C gpu_search_v42`
+    found the process with the 8 fields and the names that
+    gpu_queue.running matches (scripts/gpu_queue.py:85-98), and stage a was
+    interrupted by SIGTERM after its first batch, then resumed (its log holds
+    both runs' PROGRESS lines in one unbroken chain)."""
+    if not (FOLLOW / "ps-fields.json").exists():
+        pytest.skip("follow fixtures not generated")
+    import json
+    seen = json.loads((FOLLOW / "ps-fields.json").read_text())
+    assert seen["fields"] == 8 and seen["gpu"] == "0"
+    assert [seen["limit"], seen["first"], seen["last"]] == ["10000000", "9800000", "9812499"]
+    assert seen["results_name"] == "gpu-0a-results.txt" and seen["state_name"] == "gpu-0a-state.txt"
+    assert 1 <= seen["progress_lines_before_sigterm"] < 25
+    assert len((FOLLOW / "gpu-0a-v21-start.txt").read_text().splitlines()) == 2
+
+
+def test_gpu_follow_and_gpu_queue_run_over_gb300_checkpoints(tmp_path):
+    """The reference's supervisor loop run end to end as processes:
+    scripts/gpu_follow.py from stage b starts scripts/gpu_queue.py for every
+    stage b..cd with GPU_IDS=0.  Stage b's queue accepts GPU 0's interval of
+    stage a (interrupted and resumed) and of stage b from the checkpoints
+    the drop-in wrote, without launching anything; the later stages are
+    covered by a main-search state at root 9,412,500
+    (scripts/gpu_queue.py:194-220).  Every queue finishes and the follower
+    reaches FOLLOW FINISHED."""
+    root = _queue_root(tmp_path)
+    (root / "main-state.txt").write_text("limit 10000000\nresume 9412500\n")
+    before = {f.name: f.read_bytes() for f in root.iterdir() if f.name.startswith("gpu-0")}
+    done = _run_script(root, root / "scripts" / "gpu_follow.py", "b")
+    out = done.stdout
+    assert done.returncode == 0, (out[-2000:], done.stderr[-2000:])
+    assert out.count("FOLLOW STAGE ") == 81 and out.rstrip().endswith("FOLLOW FINISHED")
+    assert out.count("QUEUE FINISHED") == 81
+    assert "DONE gpu=0 range=9600000-9612499" in out
+    assert "ERROR" not in out and "START gpu=" not in out and "PRESERVED" not in out
+    assert "ALREADY COVERED range=9400000-9412499" in out
+    for name, data in before.items():
+        assert (root / name).read_bytes() == data, name
+
+
+def test_gpu_queue_sets_aside_a_broken_chain(tmp_path):
+    """The same queue over stage b's checkpoint with one PROGRESS line
+    dropped from its log: gpu_queue.py accepts stage a, refuses b's chain,
+    moves its state and log aside as .unverified (scripts/gpu_queue.py:70-82)
+    and goes on to launch a fresh run (no binary is installed here, so that
+    launch fails and the queue reports it and finishes)."""
+    root = _queue_root(tmp_path)
+    log = (root / "gpu-0b.log").read_text().splitlines()
+    progress = [i for i, line in enumerate(log) if line.startswith("PROGRESS")]
+    damaged = [x for i, x in enumerate(log) if i != progress[4]]
+    (root / "gpu-0b.log").write_text("".join(x + "\n" for x in damaged))
+    state = (root / "gpu-0b-state.txt").read_text()
+    done = _run_script(root, root / "scripts" / "gpu_queue.py", "b", timeout=120)
+    out = done.stdout
+    assert done.returncode == 0, (out, done.stderr)
+    assert "PRESERVED UNVERIFIED CHECKPOINT gpu-0b-state.txt" in out
+    assert "PRESERVED UNVERIFIED CHECKPOINT gpu-0b.log" in out
+    assert "ERROR gpu=0" in out and out.rstrip().endswith("QUEUE FINISHED")
+    kept = {f.name: f for f in root.iterdir()}
+    moved = [n for n in kept if n.startswith("gpu-0b-state.txt.unverified-")]
+    assert len(moved) == 1 and kept[moved[0]].read_text() == state
+    assert (root / "gpu-0a-state.txt").read_bytes() == (FOLLOW / "gpu-0a-state.txt").read_bytes()
