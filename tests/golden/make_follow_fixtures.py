@@ -46,8 +46,10 @@ def launch(root, suffix):
 
 
 def ps_fields(pid):
-    out = subprocess.run(["ps", "-C", "gpu_search_v42", "-o", "pid=,args="], text=True,
-                         capture_output=True).stdout
+    # in the queue daemon's environment: COLUMNS would cut the args column
+    env = {k: v for k, v in os.environ.items() if k not in ("COLUMNS", "LINES")}
+    out = subprocess.run(["ps", "-C", "gpu_search_v42", "-o", "pid=,args="], text=True, capture_output=True,
+                         env=env).stdout
     for line in out.splitlines():
         fields = line.split()
         if fields and fields[0] == str(pid):

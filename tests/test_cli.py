@@ -208,8 +208,11 @@ def test_queue_launch_found_by_ps(built, tmp_path):
         deadline = time.time() + 300
         while p.poll() is None and time.time() < deadline and "PROGRESS" not in (tmp_path / "gpu-0a.log").read_text():
             time.sleep(0.005)
-        out = subprocess.run(["ps", "-C", "gpu_search_v42", "-o", "pid=,args="], text=True,
-                             capture_output=True).stdout
+        # in the queue daemon's environment: COLUMNS (set under some test
+        # runners) would cut ps's args column at that width
+        env = {k: v for k, v in os.environ.items() if k not in ("COLUMNS", "LINES")}
+        out = subprocess.run(["ps", "-C", "gpu_search_v42", "-o", "pid=,args="], text=True, capture_output=True,
+                             env=env).stdout
         found = next((l.split() for l in out.splitlines() if l.split()[:1] == [str(p.pid)]), None)
     finally:
         if p.poll() is None:
