@@ -277,7 +277,8 @@ struct RowRef {
 // Work items of the given rows: each row's m-range [l, N] cut into ranges of
 // about item_target alpha*beta evaluations (at most kTileCap roots), then
 // ordered by m so that concurrently running items read the same m-side
-// records from L2.  Returns the largest row segment and m-range.
+// records from L2; the last wave is cut finer.  Returns the number of items
+// and sets *alpha_cap to the largest row segment.
 size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_cap, uint32_t min_tile) {
     const uint64_t n = h->limit;
     const uint32_t target = h->opts.item_target ? h->opts.item_target : kDefaultItemTarget;
@@ -295,7 +296,10 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
         tile[r] = tm;
         total += (n - l + 1 + tm - 1) / tm;
     }
-    if (ensure_items(h, total)) return (size_t)-1;
+    // the last wave of items (four per SM: two per CTA of the default shape)
+    // is cut in four, so that the CTAs run out of work closer together
+    const size_t tail = std::min(total, (size_t)h->sm_count * 4);
+    if (ensure_items(h, total + 3 * tail)) return (size_t)-1;
     // counting sort by m-bucket of the item start
     const size_t nb = (n >> kBucketShift) + 2;
     std::vector<uint32_t> count(nb + 1, 0);
@@ -310,8 +314,15 @@ size_t build_items(hss_t* h, const RowRef* rows, size_t nrows, uint32_t* alpha_c
                 WorkItem{(uint32_t)l, (uint32_t)m, (uint32_t)m1, rows[r].index};
         }
     }
+    std::vector<WorkItem> last(h->h_items + total - tail, h->h_items + total);
+    size_t pos = total - tail;
+    for (const WorkItem& it : last) {
+        const uint32_t q = (it.m1 - it.m0 + 3) / 4;
+        for (uint32_t s = it.m0; s < it.m1; s += q)
+            h->h_items[pos++] = WorkItem{it.l, s, std::min(s + q, it.m1), it.row};
+    }
     *alpha_cap = acap;
-    return total;
+    return pos;
 }
 
 // Constants of the call's rows (row i of the call at index i).

@@ -116,7 +116,7 @@ __device__ inline uint64_t gcd64(uint64_t a, uint64_t b) {
 }
 
 // Multiplicative inverse of an odd number mod 2^32 (Newton iteration).
-__host__ __device__ inline uint32_t inverse_odd(uint32_t d) {
+__host__ __device__ constexpr uint32_t inverse_odd(uint32_t d) {
     uint32_t x = d;  // correct to 3 bits
     for (int i = 0; i < 4; ++i) x *= 2u - d * x;
     return x;
@@ -799,12 +799,15 @@ __device__ __forceinline__ uint32_t classify(const RowInfo& R, uint32_t m, uint3
 // K terms (see shared_prime_eps_scale).
 __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uint32_t& cc_r16,
                            float eps_scale = 0x1p-20f) {
-    uint64_t m2 = m * m;
-    u128 m4 = (u128)m2 * m2;
-    i128 w = (i128)R.l4 + (i128)m4 - (i128)R.n4;
-    u128 twoL = (u128)(2 * R.l2) * m2;
-    float E = u128_to_float(twoL) * eps_scale;
-    float T2 = u128_to_float(R.l4);
+    const uint32_t m32 = (uint32_t)m;  // m <= 3e7
+    const uint64_t m2 = (uint64_t)m32 * m32;
+    const u128 m4 = (u128)m2 * m2;
+    const i128 w = (i128)R.l4 + (i128)m4 - (i128)R.n4;
+    // |z| = 2 l^2 m^2 in float from three roundings: within 2^-22 of the
+    // exact value, far inside the factor-2 margin of every eps_scale
+    const float mf = (float)m32;
+    float E = R.l2x2f * (mf * mf) * eps_scale;
+    float T2 = R.l4f;
     float e2 = E + T2 * 0x1p-22f;
     float wf = i128_to_float(w);
     float ew = E + fabsf(wf) * 0x1p-21f;
@@ -824,20 +827,23 @@ __device__ PairCtx make_ctx(const RowInfo& R, uint64_t m, uint32_t& cc_cand, uin
     }
     c.eps = E;
     c.sf = u128_to_float(R.l4 + m4);
-    bool f3 = R.l3 || m % 3 == 0;
-    bool f5 = !R.l5 && m % 5 != 0;
+    bool f3 = R.l3 || m32 % 3 == 0;
+    bool f5 = !R.l5 && m32 % 5 != 0;
     // both orientations pass the area test for every product exactly when
     // l*m is even and 3 and 5 both divide l*m (see eval_fast)
     const bool dual = (R.leven || (m & 1) == 0) && f3 && !f5;
-    c.m = (uint32_t)m | (dual ? 0x80000000u : 0u);
-    uint32_t D = 3u * (f3 ? 3u : 1u) * (f5 ? 5u : 1u);
-    c.dinv = inverse_odd(D);
-    c.dthr = 0xFFFFFFFFu / (8u * D);
-    uint32_t mA = (uint32_t)(m % kModA), mD = (uint32_t)(m % kModD);
+    c.m = m32 | (dual ? 0x80000000u : 0u);
+    // the area divisor D = 3 (f3 ? 3 : 1) (f5 ? 5 : 1): its inverse and gate
+    // threshold floor((2^32 - 1) / (8 D)) are compile-time constants
+    constexpr uint32_t kInv3 = inverse_odd(3), kInv9 = inverse_odd(9), kInv15 = inverse_odd(15),
+                       kInv45 = inverse_odd(45);
+    c.dinv = f3 ? (f5 ? kInv45 : kInv9) : (f5 ? kInv15 : kInv3);
+    c.dthr = f3 ? (f5 ? 0xFFFFFFFFu / 360u : 0xFFFFFFFFu / 72u) : (f5 ? 0xFFFFFFFFu / 120u : 0xFFFFFFFFu / 24u);
+    const uint32_t mA = m32 % kModA, mD = m32 % kModD;
     uint32_t sA = (R.lmodA + pow4_mod(mA, kModA)) % kModA;
     uint32_t sD = (R.lmodD + pow4_mod(mD, kModD)) % kModD;
     c.sres = sA | (sD << kShiftD) | (f5 ? 0x80000000u : 0u);
-    uint32_t areaA = 2u * (R.l2modA * (uint32_t)(m2 % kModA) % kModA);
+    uint32_t areaA = 2u * (R.l2modA * (mA * mA % kModA) % kModA);
     bool cc = area_gate(areaA, c.dinv, c.dthr) && w <= 0;
     cc_cand = cc ? 1u : 0u;
     cc_r16 = (cc && (sA & 15u) <= 1u) ? 1u : 0u;
@@ -1944,7 +1950,8 @@ void fill_row_info(const uint32_t* spf, const uint32_t* seg_off, uint64_t n, uin
     R->n4 = (u128)(n * n) * (n * n);
     R->lmodA = mod_u128_small(R->l4, kModA);
     R->lmodD = mod_u128_small(R->l4, kModD);
-    R->spare = 0;
+    R->l2x2f = (float)(2 * R->l2);
+    R->l4f = (float)R->l4;
     R->l2modA = (uint32_t)(R->l2 % kModA);
     R->l3 = l % 3 == 0;
     R->l5 = l % 5 == 0;

@@ -35,14 +35,15 @@ struct RowInfo {
     uint64_t l, l2;
     unsigned __int128 l4, n4;
     uint64_t fixed;             // prod of non-split p^(2a) of l
-    uint32_t lmodA, lmodD, l2modA, spare;  // l^4 mod kModA, kModD; l^2 mod kModA
+    uint32_t lmodA, lmodD, l2modA;  // l^4 mod kModA, kModD; l^2 mod kModA
+    float l2x2f;                // 2 l^2, rounded to float
     uint32_t l3, l5, leven, nodd;          // 3 | l, 5 | l, l even, number of odd primes
     uint32_t pinv[9], pthr[9];
     uint32_t psplit;            // bit i set when odd prime i is = 1 mod 4
     uint32_t free_l, seg;       // |free(l)| and the first record of l's segment
     uint32_t nsplit;            // split primes of l (increasing) with exponents
     uint32_t sp[8], se[8];
-    uint32_t pad;
+    float l4f;                  // l^4, rounded to float
 };
 
 // Exact work queued by the search kernels for exact_kernel: kind bits 0-1
