@@ -59,8 +59,6 @@ constexpr uint32_t kSlices = 8;            // plain kernel: blocks per row
 constexpr uint32_t kPlainThreads = 128;    // plain kernel: threads per block
 constexpr uint32_t kMergedThreads = 128;   // big shared-prime pairs: one CTA per pair
 constexpr uint32_t kMergedListCap = 1536;  // alpha + beta entries of one big pair
-constexpr uint32_t kWarpPairThreads = 256; // shared-prime pairs: one warp per pair
-constexpr uint32_t kWarpPairWarps = kWarpPairThreads / 32;
 constexpr uint32_t kWarpListCap = 160;     // alpha + beta entries of one warp's pair
 constexpr uint32_t kMaxTerms = 16;
 constexpr uint32_t kQueue = 64;            // events per warp queue
@@ -1023,42 +1021,44 @@ __device__ __forceinline__ void batched_pass(const AlphaHot* s_alpha, uint32_t n
         const uint32_t j = (uint32_t)ev, slot = (uint32_t)(ev >> 32) & 0xFFu, k = (uint32_t)(ev >> 40) & 0x1FFFu;
         push_hits(&buf, tags, a0 + k, j, (uint32_t)l, pair_m(wctx[slot]), row, false);
     };
-    if (FLUSH) {
+    if constexpr (FLUSH) {
         // the item's last events (the row values are replaced next)
         while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
         return;
-    }
-    for (uint32_t base = 0; base < total; base += 32) {
-        const uint32_t r = base + lane;
-        uint32_t owner = 0;
+    } else {
+        for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t r = base + lane;
+            uint32_t owner = 0;
 #pragma unroll
-        for (uint32_t step = 16; step >= 1; step >>= 1) {
-            const uint32_t v = __shfl_sync(kFull, incl, owner + step - 1);
-            if (v <= r) owner += step;
-        }
-        owner &= 31u;
-        uint32_t off = r - __shfl_sync(kFull, excl, owner);
-        uint32_t slot = owner, j = 0;
-#pragma unroll
-        for (uint32_t u = 0; u < kRootsPerLane; ++u) {
-            const uint32_t cu = __shfl_sync(kFull, cnt[u], owner);
-            const uint32_t su = __shfl_sync(kFull, s0[u], owner);
-            if (off < cu && slot == owner) {
-                slot = 32 * u + owner + 1024u;  // mark found
-                j = su + off;
+            for (uint32_t step = 16; step >= 1; step >>= 1) {
+                const uint32_t v = __shfl_sync(kFull, incl, owner + step - 1);
+                if (v <= r) owner += step;
             }
-            if (slot == owner) off -= cu;
-        }
-        slot = (slot - 1024u) & 127u;
-        const bool live = r < total;
-        const PairCtx c = wctx[slot];
-        const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
-        const bool cb = (b.rre & kCentralBit) != 0;
-        for (uint32_t k = 0; k < na; ++k) {
-            const AlphaHot a = s_alpha[k];
-            uint32_t flags = 0;
-            if (live) flags = eval_fast<DUAL ? 1 : 0, true, true>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
-            if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags))) drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
+            owner &= 31u;
+            uint32_t off = r - __shfl_sync(kFull, excl, owner);
+            uint32_t slot = owner, j = 0;
+#pragma unroll
+            for (uint32_t u = 0; u < kRootsPerLane; ++u) {
+                const uint32_t cu = __shfl_sync(kFull, cnt[u], owner);
+                const uint32_t su = __shfl_sync(kFull, s0[u], owner);
+                if (off < cu && slot == owner) {
+                    slot = 32 * u + owner + 1024u;  // mark found
+                    j = su + off;
+                }
+                if (slot == owner) off -= cu;
+            }
+            slot = (slot - 1024u) & 127u;
+            const bool live = r < total;
+            const PairCtx c = wctx[slot];
+            const HotRec b = live ? cache.hot[j] : HotRec{0.f, 0.f, kCentralBit, 0u};
+            const bool cb = (b.rre & kCentralBit) != 0;
+            for (uint32_t k = 0; k < na; ++k) {
+                const AlphaHot a = s_alpha[k];
+                uint32_t flags = 0;
+                if (live) flags = eval_fast<DUAL ? 1 : 0, true, true>(a, b.re, b.im, b.rre, b.rim, cb, c, s_tab, acc);
+                if (queue_push(q, qn, flags != 0, batched_event_word(j, slot, k, flags)))
+                    drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
+            }
         }
     }
 }
