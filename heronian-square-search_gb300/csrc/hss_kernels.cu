@@ -1530,8 +1530,9 @@ __global__ void __launch_bounds__(128) merged_setup_kernel(const DeviceCache cac
 // Shared-prime pairs of one chunk, a segment of pairs per warp at a time.  A
 // warp claims blocks of 32 consecutive descriptors from the chunk's cursor
 // (pair sizes vary widely) and stages up to kSegSlots of them in its shared
-// slice; consecutive staged pairs whose lists fit the warp's list arena form
-// a segment.  The segment's lists are built side by side (float and residue
+// slice, copying the next group's descriptors with asynchronous copies while
+// the current group runs; consecutive staged pairs whose lists fit the
+// warp's list arena form a segment.  The segment's lists are built side by side (float and residue
 // products of the prime-power values), and all its (alpha, beta)
 // combinations - the pairs' combination spaces laid end to end - run in
 // lockstep rounds of 32: each lane steps from pair to pair, so rounds stay
@@ -1576,6 +1577,7 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
     __shared__ __align__(16) AlphaHot s_list[kPairWarps][kSegList];
     __shared__ uint32_t s_queue[kPairWarps][kQueue];
     __shared__ SegSlot s_slot[kPairWarps][kSegSlots];
+    __shared__ __align__(16) uint4 s_raw[kPairWarps][kSegSlots * kDescWords];  // the next group, in flight
     // dynamic: root requests, then the wide tables
     extern __shared__ __align__(16) unsigned char s_dyn[];
     RootReq* s_req = reinterpret_cast<RootReq*>(s_dyn);
@@ -1593,164 +1595,192 @@ __global__ void __launch_bounds__(kPairWarps * 32, 2) merged_kernel(const Device
     RootReq* wreq = s_req + warp * 32 * kReqPerLane;
     const uint32_t limit = (uint32_t)cache.limit;
     uint32_t qn = 0;
-    for (;;) {
-        uint32_t b0 = 0;
-        if (lane == 0) b0 = atomicAdd(buf.desc_next, 32u);
-        b0 = __shfl_sync(kFull, b0, 0);
-        if (b0 >= n) break;
-        const uint32_t b1 = min(b0 + 32, n);
-        for (uint32_t s0 = b0; s0 < b1; s0 += kSegSlots) {
-            const uint32_t ns = min(kSegSlots, b1 - s0);
-            // staged with the dual pairs (both orientations live) first, so
-            // that a segment's rounds mix dual and single-orientation lanes
-            // at one boundary at most (word 2 of a descriptor holds ctx.m,
-            // whose bit 31 is the dual flag)
-            const bool dual_i =
-                lane < ns && (buf.pair_desc[(size_t)(s0 + lane) * kBigEntryWords + 2].w >> 31) != 0;
-            const uint32_t dmask = __ballot_sync(kFull, dual_i), vmask = (1u << ns) - 1u;
-            auto dest = [&](uint32_t i) {
-                const uint32_t below = (1u << i) - 1u;
-                return ((dmask >> i) & 1u) ? (uint32_t)__popc(dmask & below)
-                                           : (uint32_t)(__popc(dmask) + __popc(~dmask & vmask & below));
-            };
-            __syncwarp();
-            for (uint32_t w = lane; w < ns * kDescWords; w += 32)
-                reinterpret_cast<uint4*>(desc)[dest(w / kDescWords) * kDescWords + w % kDescWords] =
-                    buf.pair_desc[(size_t)(s0 + w / kDescWords) * kBigEntryWords + w % kDescWords];
-            __syncwarp();
-            for (uint32_t first = 0; first < ns;) {
-                // the segment: staged pairs first .. last - 1 whose lists fit the arena
-                uint32_t entries = 0, combos = 0;
-                if (lane >= first && lane < ns && desc[lane].state == 1) {
-                    const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
-                    entries = na + nb;
-                    combos = na * nb;
-                }
-                uint32_t incl = entries;
-#pragma unroll
-                for (int d = 1; d < (int)kSegSlots; d <<= 1) {
-                    const uint32_t t = __shfl_up_sync(kFull, incl, d);
-                    if (lane >= (uint32_t)d) incl += t;
-                }
-                const uint32_t fits = __ballot_sync(kFull, lane >= first && lane < ns && incl <= kSegList);
-                const uint32_t last = first + __popc(fits);
-                uint32_t total = combos;
-                if (lane >= first && lane < last) {
-                    slot[lane].size = combos;
-                    slot[lane].loff = incl - entries;
-                    slot[lane].cand = 0;
-                    slot[lane].r16 = 0;
-                    if (combos) {
-                        const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
-                        slot[lane].nab = na | nb << 16;
-                        slot[lane].step = seg_step(nb);
-                    }
-                } else {
-                    total = 0;
-                }
-                const uint32_t built = __shfl_sync(kFull, incl, last - 1);
-                total = __reduce_add_sync(kFull, total);
-                __syncwarp();
-                // lists of the segment, entry e of the arena by lane e mod 32
-                for (uint32_t e = lane; e < built; e += 32) {
-                    uint32_t k = first;
-                    while (k + 1 < last && e >= slot[k + 1].loff) ++k;
-                    const uint32_t idx = e - slot[k].loff, na = desc[k].free_count[0] + 1;
-                    desc_value_hot(cache, desc[k], idx < na ? 0 : 1, idx < na ? idx : idx - na, list[e]);
-                }
-                __syncwarp();
-                auto handle = [&](uint32_t ev, RootReq* slots) -> uint32_t {
-                    const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
-                    if (!index_ok(k, last, buf.error_flags) || k < first) return 0u;
-                    const PairDesc& D = desc[k];
-                    const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1, la = slot[k].loff;
-                    if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
-                    const uint2 r = merged_event(ev >> 24, list[la + ka], list[la + na + kb], D.ctx, ka, kb, D.l, D.row,
-                                                 s_tab, kTabD2, limit, &buf, slots);
-                    if (r.x & 0xFFFFu) atomicAdd(&slot[k].cand, r.x & 0xFFFFu);
-                    if (r.y) atomicAdd(&slot[k].r16, r.y);
-                    return r.x >> 16;
-                };
-                auto hit = [&](uint32_t ev, uint32_t tags) {
-                    const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
-                    if (k >= first && k < last)
-                        push_hits(&buf, tags, ka, kb, desc[k].l, pair_m(desc[k].ctx), desc[k].row, true);
-                };
-                // the lane's position: slot k, offset off in it, (ka, kb) = (off / nb, off mod nb)
-                uint32_t k = first, off = lane, size = 0, na = 1, nb = 1, la = 0, ka = 0, kb = 0, q32 = 0, r32 = 0;
-                PairCtx c{};
-                bool dual = false;
-                Acc acc{0, 0, 0, 0, 0, 0};
-                auto enter = [&]() {
-                    while (k < last && off >= slot[k].size) {
-                        off -= slot[k].size;
-                        ++k;
-                    }
-                    if (k < last) {
-                        const uint32_t nab = slot[k].nab, st = slot[k].step;
-                        size = slot[k].size;
-                        na = nab & 0xFFFFu;
-                        nb = nab >> 16;
-                        la = slot[k].loff;
-                        ka = (off * (st & 0x1FFFFu)) >> 16;  // off < 32 here (see seg_step)
-                        kb = off - ka * nb;
-                        q32 = (st >> 17) & 63u;
-                        r32 = st >> 23;
-                        c = desc[k].ctx;
-                        dual = pair_dual(c);
-                    }
-                };
-                enter();
-                for (uint32_t base = 0; base < total; base += 32) {
-                    uint32_t flags = 0;
-                    if (k < last) {
-                        const AlphaHot a = list[la + ka], bh = list[la + na + kb];
-                        flags = eval_fast<2, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc,
-                                                   dual);
-                    }
-                    if (queue_push(q, qn, flags != 0, seg_event(kb, ka, k, flags)))
-                        drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
-                    if (k < last) {
-                        off += 32;
-                        if (off < size) {
-                            ka += q32;
-                            kb += r32;
-                            if (kb >= nb) {
-                                kb -= nb;
-                                ++ka;
-                            }
-                        } else {
-                            if (acc.cand) atomicAdd(&slot[k].cand, acc.cand);
-                            if (acc.r16) atomicAdd(&slot[k].r16, acc.r16);
-                            acc.cand = acc.r16 = 0;
-                            enter();
-                        }
-                    }
-                }
-                while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
-                __syncwarp();
-                // the segment's pairs to their rows
-                if (lane >= first && lane < last && desc[lane].state == 1) {
-                    const PairDesc& D = desc[lane];
-                    const uint64_t pa = D.free_count[0] + 1, pb = D.free_count[1] + 1;
-                    const uint64_t cand = slot[lane].cand + (D.cc & 1u), r16 = slot[lane].r16 + ((D.cc >> 1) & 1u);
-                    const uint64_t prod = pair_products((uint32_t)pa, (uint32_t)pb);
-                    RowCounts* rc = &buf.rows[D.row];
-                    if (cand) {
-                        atomicAdd(&rc->candidates, (unsigned long long)cand);
-                        atomicAdd(&rc->mcandidates, (unsigned long long)cand);
-                    }
-                    if (r16) {
-                        atomicAdd(&rc->r16, (unsigned long long)r16);
-                        atomicAdd(&rc->mr16, (unsigned long long)r16);
-                    }
-                    atomicAdd(&rc->products, (unsigned long long)prod);
-                    atomicAdd(&rc->mproducts, (unsigned long long)prod);
-                }
-                __syncwarp();
-                first = last;
-            }
+    // groups of up to kSegSlots descriptors, from blocks of 32 taken from the
+    // cursor; the next group's descriptors are copied into s_raw while the
+    // current one runs (asynchronous copies, one 16-byte word per lane)
+    uint4* raw = s_raw[warp];
+    uint32_t cb0 = 0, coff = 0;
+    auto claim = [&]() {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(buf.desc_next, 32u);
+        cb0 = __shfl_sync(kFull, b, 0);
+        coff = 0;
+    };
+    auto take = [&](uint32_t& g0, uint32_t& gn) -> bool {
+        if (cb0 >= n) return false;
+        const uint32_t b1 = min(cb0 + 32, n);
+        g0 = cb0 + coff;
+        gn = min(kSegSlots, b1 - g0);
+        coff += kSegSlots;
+        if (cb0 + coff >= b1) claim();
+        return true;
+    };
+    auto prefetch = [&](uint32_t g0, uint32_t gn) {
+        for (uint32_t w = lane; w < gn * kDescWords; w += 32) {
+            const uint4* src = buf.pair_desc + (size_t)(g0 + w / kDescWords) * kBigEntryWords + w % kDescWords;
+            const uint32_t dst = (uint32_t)__cvta_generic_to_shared(raw + w);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
         }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    claim();
+    uint32_t g0 = 0, ns = 0;
+    bool have = take(g0, ns);
+    if (have) prefetch(g0, ns);
+    while (have) {
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncwarp();
+        // staged with the dual pairs (both orientations live) first, so
+        // that a segment's rounds mix dual and single-orientation lanes
+        // at one boundary at most (word 2 of a descriptor holds ctx.m,
+        // whose bit 31 is the dual flag)
+        const bool dual_i = lane < ns && (raw[lane * kDescWords + 2].w >> 31) != 0;
+        const uint32_t dmask = __ballot_sync(kFull, dual_i), vmask = (1u << ns) - 1u;
+        auto dest = [&](uint32_t i) {
+            const uint32_t below = (1u << i) - 1u;
+            return ((dmask >> i) & 1u) ? (uint32_t)__popc(dmask & below)
+                                       : (uint32_t)(__popc(dmask) + __popc(~dmask & vmask & below));
+        };
+        for (uint32_t w = lane; w < ns * kDescWords; w += 32)
+            reinterpret_cast<uint4*>(desc)[dest(w / kDescWords) * kDescWords + w % kDescWords] = raw[w];
+        __syncwarp();
+        uint32_t n0 = 0, nn = 0;
+        const bool more = take(n0, nn);
+        if (more) prefetch(n0, nn);
+        for (uint32_t first = 0; first < ns;) {
+            // the segment: staged pairs first .. last - 1 whose lists fit the arena
+            uint32_t entries = 0, combos = 0;
+            if (lane >= first && lane < ns && desc[lane].state == 1) {
+                const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
+                entries = na + nb;
+                combos = na * nb;
+            }
+            uint32_t incl = entries;
+#pragma unroll
+            for (int d = 1; d < (int)kSegSlots; d <<= 1) {
+                const uint32_t t = __shfl_up_sync(kFull, incl, d);
+                if (lane >= (uint32_t)d) incl += t;
+            }
+            const uint32_t fits = __ballot_sync(kFull, lane >= first && lane < ns && incl <= kSegList);
+            const uint32_t last = first + __popc(fits);
+            uint32_t total = combos;
+            if (lane >= first && lane < last) {
+                slot[lane].size = combos;
+                slot[lane].loff = incl - entries;
+                slot[lane].cand = 0;
+                slot[lane].r16 = 0;
+                if (combos) {
+                    const uint32_t na = desc[lane].free_count[0] + 1, nb = desc[lane].free_count[1] + 1;
+                    slot[lane].nab = na | nb << 16;
+                    slot[lane].step = seg_step(nb);
+                }
+            } else {
+                total = 0;
+            }
+            const uint32_t built = __shfl_sync(kFull, incl, last - 1);
+            total = __reduce_add_sync(kFull, total);
+            __syncwarp();
+            // lists of the segment, entry e of the arena by lane e mod 32
+            for (uint32_t e = lane; e < built; e += 32) {
+                uint32_t k = first;
+                while (k + 1 < last && e >= slot[k + 1].loff) ++k;
+                const uint32_t idx = e - slot[k].loff, na = desc[k].free_count[0] + 1;
+                desc_value_hot(cache, desc[k], idx < na ? 0 : 1, idx < na ? idx : idx - na, list[e]);
+            }
+            __syncwarp();
+            auto handle = [&](uint32_t ev, RootReq* slots) -> uint32_t {
+                const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
+                if (!index_ok(k, last, buf.error_flags) || k < first) return 0u;
+                const PairDesc& D = desc[k];
+                const uint32_t na = D.free_count[0] + 1, nb = D.free_count[1] + 1, la = slot[k].loff;
+                if (!index_ok(ka, na, buf.error_flags) || !index_ok(kb, nb, buf.error_flags)) return 0u;
+                const uint2 r = merged_event(ev >> 24, list[la + ka], list[la + na + kb], D.ctx, ka, kb, D.l, D.row,
+                                             s_tab, kTabD2, limit, &buf, slots);
+                if (r.x & 0xFFFFu) atomicAdd(&slot[k].cand, r.x & 0xFFFFu);
+                if (r.y) atomicAdd(&slot[k].r16, r.y);
+                return r.x >> 16;
+            };
+            auto hit = [&](uint32_t ev, uint32_t tags) {
+                const uint32_t kb = ev & 0xFFu, ka = (ev >> 8) & 0xFFu, k = (ev >> 16) & 0xFFu;
+                if (k >= first && k < last)
+                    push_hits(&buf, tags, ka, kb, desc[k].l, pair_m(desc[k].ctx), desc[k].row, true);
+            };
+            // the lane's position: slot k, offset off in it, (ka, kb) = (off / nb, off mod nb)
+            uint32_t k = first, off = lane, size = 0, na = 1, nb = 1, la = 0, ka = 0, kb = 0, q32 = 0, r32 = 0;
+            PairCtx c{};
+            bool dual = false;
+            Acc acc{0, 0, 0, 0, 0, 0};
+            auto enter = [&]() {
+                while (k < last && off >= slot[k].size) {
+                    off -= slot[k].size;
+                    ++k;
+                }
+                if (k < last) {
+                    const uint32_t nab = slot[k].nab, st = slot[k].step;
+                    size = slot[k].size;
+                    na = nab & 0xFFFFu;
+                    nb = nab >> 16;
+                    la = slot[k].loff;
+                    ka = (off * (st & 0x1FFFFu)) >> 16;  // off < 32 here (see seg_step)
+                    kb = off - ka * nb;
+                    q32 = (st >> 17) & 63u;
+                    r32 = st >> 23;
+                    c = desc[k].ctx;
+                    dual = pair_dual(c);
+                }
+            };
+            enter();
+            for (uint32_t base = 0; base < total; base += 32) {
+                uint32_t flags = 0;
+                if (k < last) {
+                    const AlphaHot a = list[la + ka], bh = list[la + na + kb];
+                    flags = eval_fast<2, true>(a, bh.re, bh.im, bh.ra, bh.ia, (bh.ra >> 31) != 0, c, s_tab, acc,
+                                               dual);
+                }
+                if (queue_push(q, qn, flags != 0, seg_event(kb, ka, k, flags)))
+                    drain(q, qn, 32, wreq, buf.error_flags, handle, hit);
+                if (k < last) {
+                    off += 32;
+                    if (off < size) {
+                        ka += q32;
+                        kb += r32;
+                        if (kb >= nb) {
+                            kb -= nb;
+                            ++ka;
+                        }
+                    } else {
+                        if (acc.cand) atomicAdd(&slot[k].cand, acc.cand);
+                        if (acc.r16) atomicAdd(&slot[k].r16, acc.r16);
+                        acc.cand = acc.r16 = 0;
+                        enter();
+                    }
+                }
+            }
+            while (qn) drain(q, qn, qn < 32 ? qn : 32, wreq, buf.error_flags, handle, hit);
+            __syncwarp();
+            // the segment's pairs to their rows
+            if (lane >= first && lane < last && desc[lane].state == 1) {
+                const PairDesc& D = desc[lane];
+                const uint64_t pa = D.free_count[0] + 1, pb = D.free_count[1] + 1;
+                const uint64_t cand = slot[lane].cand + (D.cc & 1u), r16 = slot[lane].r16 + ((D.cc >> 1) & 1u);
+                const uint64_t prod = pair_products((uint32_t)pa, (uint32_t)pb);
+                RowCounts* rc = &buf.rows[D.row];
+                if (cand) {
+                    atomicAdd(&rc->candidates, (unsigned long long)cand);
+                    atomicAdd(&rc->mcandidates, (unsigned long long)cand);
+                }
+                if (r16) {
+                    atomicAdd(&rc->r16, (unsigned long long)r16);
+                    atomicAdd(&rc->mr16, (unsigned long long)r16);
+                }
+                atomicAdd(&rc->products, (unsigned long long)prod);
+                atomicAdd(&rc->mproducts, (unsigned long long)prod);
+            }
+            __syncwarp();
+            first = last;
+        }
+        ns = nn;
+        have = more;
     }
 }
 
