@@ -1451,11 +1451,6 @@ __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint
 // of group_value, with the block sizes recomputed from the exponents).
 __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int g, uint32_t k, AlphaHot& out) {
     const uint32_t count = D.count[g];
-    uint32_t suffix[kDescTerms];
-    for (int i = (int)count - 1, acc = 1; i >= 0; --i) {
-        suffix[i] = (uint32_t)acc;
-        acc *= 4 * (int)D.e[g][i] + 1;
-    }
     float xr = g == 0 ? D.scale_f : 1.f, xi = 0.f;
     uint32_t rr = g == 0 ? D.scale_res : kResOne, ri = 0u;
     auto mul = [&](const HotRec& v) {
@@ -1468,6 +1463,33 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
         ri = yi;
     };
     const bool central = k >= D.free_count[g];
+    if (count <= 2) {
+        // the common short sides, decoded directly.  One term: entry k is
+        // scale v_0[k] (k = 2 e_0 is the central value).  Two terms: block 0
+        // holds scale v_0[k / s_1] v_1[k mod s_1] for k < 2 e_0 s_1, then
+        // scale v_0[2 e_0] v_1[k - 2 e_0 s_1] up to the central value.
+        if (count >= 1) {
+            const uint32_t two_e0 = 2u * D.e[g][0];
+            if (count == 1) {
+                mul(cache.pp_hot[D.base[g][0] + k]);
+            } else {
+                const uint32_t s1 = 4u * D.e[g][1] + 1u, block0 = two_e0 * s1;
+                const uint32_t r = k < block0 ? k / s1 : two_e0;
+                mul(cache.pp_hot[D.base[g][0] + r]);
+                mul(cache.pp_hot[D.base[g][1] + (k < block0 ? k - r * s1 : k - block0)]);
+            }
+        }
+        out.re = xr;
+        out.im = xi;
+        out.ra = rr | (central ? kCentralBit : 0u);
+        out.ia = ri;
+        return;
+    }
+    uint32_t suffix[kDescTerms];
+    for (int i = (int)count - 1, acc = 1; i >= 0; --i) {
+        suffix[i] = (uint32_t)acc;
+        acc *= 4 * (int)D.e[g][i] + 1;
+    }
     uint32_t i = 0;
     if (!central) {
         while (k >= 2u * D.e[g][i] * suffix[i]) {
