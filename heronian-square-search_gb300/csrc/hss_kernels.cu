@@ -1463,21 +1463,44 @@ __device__ void desc_value_hot(const DeviceCache& cache, const PairDesc& D, int 
         ri = yi;
     };
     const bool central = k >= D.free_count[g];
-    if (count <= 2) {
-        // the common short sides, decoded directly.  One term: entry k is
-        // scale v_0[k] (k = 2 e_0 is the central value).  Two terms: block 0
-        // holds scale v_0[k / s_1] v_1[k mod s_1] for k < 2 e_0 s_1, then
-        // scale v_0[2 e_0] v_1[k - 2 e_0 s_1] up to the central value.
-        if (count >= 1) {
+    if (count <= 3) {
+        // sides of up to three terms (every side of a warp-sized pair),
+        // decoded directly into one digit per term (s_j = 4 e_j + 1, the
+        // central digit 2 e_j).  One term: entry k is scale v_0[k], k = 2 e_0
+        // being the central value.  Two terms: block 0 holds
+        // scale v_0[k / s_1] v_1[k mod s_1] for k < 2 e_0 s_1, then
+        // scale v_0[2 e_0] v_1[k - 2 e_0 s_1] up to the central value.  Three
+        // terms: the same with the last two digits in mixed radix (s_1, s_2)
+        // in block 0, then block 1 (digits 2 e_0, r, d_2), then the last
+        // term's digits after 2 e_0, 2 e_1.
+        if (count == 1) {
+            mul(cache.pp_hot[D.base[g][0] + k]);
+        } else if (count == 2) {
             const uint32_t two_e0 = 2u * D.e[g][0];
-            if (count == 1) {
-                mul(cache.pp_hot[D.base[g][0] + k]);
+            const uint32_t s1 = 4u * D.e[g][1] + 1u, block0 = two_e0 * s1;
+            const uint32_t r = k < block0 ? k / s1 : two_e0;
+            mul(cache.pp_hot[D.base[g][0] + r]);
+            mul(cache.pp_hot[D.base[g][1] + (k < block0 ? k - r * s1 : k - block0)]);
+        } else if (count == 3) {
+            const uint32_t two_e0 = 2u * D.e[g][0], two_e1 = 2u * D.e[g][1];
+            const uint32_t s1 = 2u * two_e1 + 1u, s2 = 4u * D.e[g][2] + 1u;
+            const uint32_t block0 = two_e0 * s1 * s2, block1 = two_e1 * s2;
+            uint32_t d0 = two_e0, d1 = two_e1, d2;
+            if (k < block0) {
+                const uint32_t q = k / s2;
+                d2 = k - q * s2;
+                d0 = q / s1;
+                d1 = q - d0 * s1;
+            } else if (k < block0 + block1) {
+                const uint32_t k1 = k - block0;
+                d1 = k1 / s2;
+                d2 = k1 - d1 * s2;
             } else {
-                const uint32_t s1 = 4u * D.e[g][1] + 1u, block0 = two_e0 * s1;
-                const uint32_t r = k < block0 ? k / s1 : two_e0;
-                mul(cache.pp_hot[D.base[g][0] + r]);
-                mul(cache.pp_hot[D.base[g][1] + (k < block0 ? k - r * s1 : k - block0)]);
+                d2 = k - block0 - block1;
             }
+            mul(cache.pp_hot[D.base[g][0] + d0]);
+            mul(cache.pp_hot[D.base[g][1] + d1]);
+            mul(cache.pp_hot[D.base[g][2] + d2]);
         }
         out.re = xr;
         out.im = xi;
