@@ -121,6 +121,59 @@ def test_area_gate_rotation_identity():
             assert (rot <= thr) == (n % q == 0), (d, n)
 
 
+def _generic_digits(k, exps):
+    """A side's list entry k as one digit per term, decoded the general way
+    (block of the first non-central term, then mixed radix over the later
+    terms, the last one fastest); the central entry has every digit 2e."""
+    sizes = [4 * e + 1 for e in exps]
+    suffix = [math.prod(sizes[j + 1:]) for j in range(len(exps))]
+    free = sum(2 * e * suffix[i] for i, e in enumerate(exps))
+    if k >= free:
+        return [2 * e for e in exps]
+    i = 0
+    while k >= 2 * exps[i] * suffix[i]:
+        k -= 2 * exps[i] * suffix[i]
+        i += 1
+    digits = [2 * e for e in exps[:i]] + [k // suffix[i]]
+    rem = k % suffix[i]
+    for j in range(i + 1, len(exps)):
+        digits.append(rem // suffix[j])
+        rem %= suffix[j]
+    return digits
+
+
+def _direct_digits(k, exps):
+    """The same for sides of one to three terms, in the form the warp kernel's
+    list build computes it (no block search, no suffix table)."""
+    if len(exps) == 1:
+        return [k]
+    if len(exps) == 2:
+        s1, block0 = 4 * exps[1] + 1, 2 * exps[0] * (4 * exps[1] + 1)
+        r = k // s1 if k < block0 else 2 * exps[0]
+        return [r, k - r * s1 if k < block0 else k - block0]
+    s1, s2 = 4 * exps[1] + 1, 4 * exps[2] + 1
+    block0, block1 = 2 * exps[0] * s1 * s2, 2 * exps[1] * s2
+    if k < block0:
+        q = k // s2
+        return [q // s1, q % s1, k - q * s2]
+    if k < block0 + block1:
+        return [2 * exps[0], (k - block0) // s2, (k - block0) % s2]
+    return [2 * exps[0], 2 * exps[1], k - block0 - block1]
+
+
+def test_direct_list_decode_matches_general_decode():
+    """Every entry of every side of one to three terms (exponents 1..4, the
+    central entry included) gets the same digits from the direct decode of
+    the warp kernel's list build as from the general decode that the big-pair
+    kernel and the exact path use, so both build the same values."""
+    import itertools
+    for count in (1, 2, 3):
+        for exps in itertools.product(range(1, 5), repeat=count):
+            entries = (math.prod(4 * e + 1 for e in exps) - 1) // 2 + 1
+            for k in range(entries):
+                assert _direct_digits(k, list(exps)) == _generic_digits(k, list(exps)), (exps, k)
+
+
 def test_partition_rows_balances_pairs():
     parts = hss.partition_rows(10 ** 7, 7500000, 7500511, 4)
     assert parts[0][0] == 7500000 and parts[-1][1] == 7500511
