@@ -1318,18 +1318,14 @@ __device__ __noinline__ uint2 merged_event(uint32_t flags, AlphaHot a, AlphaHot 
     return make_uint2(r.x | (r.z << 16) | (r.w << 20), r.y);
 }
 
-// Splits the merged terms of (l, m) into two groups (largest terms first,
-// each to the group with the smaller product of sizes).  ok = 1: fits
-// list_cap; 2: too big for it; 0: an exponent beyond the prime-power table.
-__device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, MergedShared& S,
-                             uint32_t list_cap) {
-    const uint64_t m = q.y;
-    S.l = q.x;
-    S.m = m;
-    S.row = q.z;
-    S.ok = 1;
+// The merged terms of pair (l, m): the split primes of l and of m, with the
+// exponents added where both have the prime, and the term order that splits
+// them into two groups (decreasing exponent, stable); fixed gets
+// 2 fixed(l) fixed(m), the real factor of every value.  Returns the count.
+__device__ uint32_t merged_terms(const DeviceCache& cache, const RowInfo& R, uint64_t m, uint32_t (&tp)[kMaxTerms],
+                                 uint32_t (&te)[kMaxTerms], uint32_t (&order)[kMaxTerms], i128& fixed) {
     uint32_t mp[9], me[9], nm = 0;
-    i128 fixed = (i128)2 * (i128)R.fixed;
+    fixed = (i128)2 * (i128)R.fixed;
     uint32_t x = (uint32_t)m;  // m <= 3e7: 32-bit divisions
     while (x > 1) {
         uint32_t p = cache.spf[x], a = 0;
@@ -1344,7 +1340,7 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
             for (uint32_t t = 0; t < 2 * a; ++t) fixed *= p;
         }
     }
-    uint32_t tp[kMaxTerms], te[kMaxTerms], count = 0;
+    uint32_t count = 0;
     uint32_t i = 0, j = 0;
     while (i < R.nsplit || j < nm) {
         if (j == nm || (i < R.nsplit && R.sp[i] < mp[j])) {
@@ -1358,7 +1354,6 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
             te[count++] = R.se[i++] + me[j++];
         }
     }
-    uint32_t order[kMaxTerms];
     for (uint32_t t = 0; t < count; ++t) order[t] = t;
     for (uint32_t a = 1; a < count; ++a)
         for (uint32_t b = a; b > 0 && te[order[b]] > te[order[b - 1]]; --b) {
@@ -1366,6 +1361,22 @@ __device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q
             order[b] = order[b - 1];
             order[b - 1] = tmp;
         }
+    return count;
+}
+
+// Splits the merged terms of (l, m) into two groups (largest terms first,
+// each to the group with the smaller product of sizes), with the block and
+// suffix tables of the exact path's decode.  ok = 1: fits list_cap; 2: too
+// big for it; 0: an exponent beyond the prime-power table.
+__device__ void merged_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, MergedShared& S,
+                             uint32_t list_cap) {
+    S.l = q.x;
+    S.m = q.y;
+    S.row = q.z;
+    S.ok = 1;
+    uint32_t tp[kMaxTerms], te[kMaxTerms], order[kMaxTerms];
+    i128 fixed;
+    const uint32_t count = merged_terms(cache, R, q.y, tp, te, order, fixed);
     uint64_t wsz[2] = {1, 1};
     S.g[0].count = S.g[1].count = 0;
     for (uint32_t t = 0; t < count; ++t) {
@@ -1423,27 +1434,44 @@ static_assert(sizeof(PairDesc) <= kBigEntryWords * 16 && sizeof(PairDesc) % 16 =
 // window decision and root window of the pair is taken against it.
 __device__ __forceinline__ float shared_prime_eps_scale(uint32_t K) { return (float)(12 + 8 * K) * 0x1p-24f; }
 
+// The descriptor of a shared-prime pair: the groups of merged_setup written
+// straight into it (a group of value count w has (w - 1) / 2 free values,
+// the sum of its blocks), without the block and suffix tables that only the
+// exact path's decode needs.
 __device__ void pair_desc_setup(const DeviceCache& cache, const RowInfo& R, uint4 q, PairDesc& D, uint32_t cap) {
-    MergedShared S;
-    merged_setup(cache, R, q, S, cap);
+    uint32_t tp[kMaxTerms], te[kMaxTerms], order[kMaxTerms];
+    i128 fixed;
+    const uint32_t count = merged_terms(cache, R, q.y, tp, te, order, fixed);
     D.l = q.x;
     D.m = q.y;
     D.row = q.z;
-    D.state = S.ok == 1 ? 1 : (S.ok == 2 ? 2 : 3);
-    if (S.g[0].count > kDescTerms || S.g[1].count > kDescTerms) D.state = 3;
-    if (D.state == 3) return;
-    for (int g = 0; g < 2; ++g) {
-        D.count[g] = (uint8_t)S.g[g].count;
-        D.free_count[g] = S.g[g].free_count;
-        for (uint32_t t = 0; t < S.g[g].count; ++t) {
-            D.base[g][t] = S.g[g].base[t];
-            D.e[g][t] = (uint8_t)S.g[g].e[t];
+    uint64_t wsz[2] = {1, 1};
+    uint32_t n[2] = {0, 0};
+    bool ok = true;
+    for (uint32_t t = 0; t < count; ++t) {
+        const uint32_t idx = order[t];
+        const int side = wsz[0] <= wsz[1] ? 0 : 1;
+        if (n[side] < kDescTerms) {
+            D.base[side][n[side]] = cache.pp_base[tp[idx]] + pp_exponent_offset(te[idx]);
+            D.e[side][n[side]] = (uint8_t)te[idx];
+        } else {
+            ok = false;  // more terms than a descriptor holds
         }
+        ++n[side];
+        wsz[side] *= 4 * te[idx] + 1;
+        if (te[idx] > cache.max_exponent) ok = false;
     }
-    D.scale_f = S.g[0].scale_f;
-    D.scale_res = S.g[0].scale_res;
+    const uint32_t free0 = (uint32_t)((wsz[0] - 1) / 2), free1 = (uint32_t)((wsz[1] - 1) / 2);
+    D.state = !ok ? 3 : (free0 + free1 + 2 > cap ? 2 : 1);
+    if (D.state == 3) return;
+    D.count[0] = (uint8_t)n[0];
+    D.count[1] = (uint8_t)n[1];
+    D.free_count[0] = free0;
+    D.free_count[1] = free1;
+    D.scale_f = i128_to_float(fixed);
+    D.scale_res = pack_residues(fixed);
     uint32_t cc_c, cc_r;
-    D.ctx = make_ctx(R, q.y, cc_c, cc_r, shared_prime_eps_scale(S.g[0].count + S.g[1].count));
+    D.ctx = make_ctx(R, q.y, cc_c, cc_r, shared_prime_eps_scale(count));
     D.cc = (uint8_t)(cc_c | (cc_r << 1));
 }
 
